@@ -1,0 +1,369 @@
+#!/usr/bin/env python3
+"""Benchmark of the FDTD task-graph hot path on GB300.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+
+One bench step is one complete solve of the workload (all of its time steps).  Default workload:
+the plain FDTD graph at 256^3 FP32 (8 seeded dielectric boxes, eps_r 1-10, 8-64 cells, PEC walls,
+Courant 0.5, Gaussian Ez source, 1000 steps).  Prints one JSON line (rank 0):
+
+  value  Mcell-updates/s with the inputs already resident in HBM (device events around the solves)
+  e2e    the same metric through the public C-ABI path with pinned host buffers, the H2D upload of the
+         inputs and the D2H download of the six result fields inside the timed region
+  roofline  the fused step kernel against measured HBM bandwidth, 64 algorithmic bytes per cell update
+  cpu_baseline  the CPU oracle (our FP32 port of the reference's fdtd_cpu, OpenMP over all host cores)
+                timed on a bounded sample of the same workload
+
+--impl reference times the reference's CPU implementation of the path instead (the oracle port; the
+reference's own build needs its source tree, which is absent where this runs) on the same workload.
+Under torchrun each rank runs an independent replica (the path shards by instance; no collective on
+the data path) and rank 0 reports the whole-job aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+BYTES_PER_CELL = 64          # 6 fields read + written (48 B) + 4 coefficients read (16 B), FP32
+FALLBACK_HBM_GBS = 6800.0
+
+WORKLOADS = {
+    # BASELINE configs[1]
+    "plain256": dict(shape=(256, 256, 256), boxes=8, eps=(1.0, 10.0), box=(8, 64), steps=1000,
+                     desc="plain FDTD graph 256^3 FP32, 8 seeded dielectric boxes (eps_r 1-10, edges 8-64), "
+                          "PEC walls, Courant 0.5, Gaussian Ez source at centre, 1000 steps"),
+    # BASELINE configs[2]
+    "large": dict(shape=(512, 512, 384), boxes=32, eps=(1.0, 10.0), box=(8, 64), steps=500,
+                  desc="large plain FDTD 512x512x384 FP32, 32 seeded dielectric boxes, 500 steps"),
+    # BASELINE configs[0] (the CPU-runnable case), used for quick checks
+    "cpu32": dict(shape=(32, 32, 32), boxes=2, eps=(2.0, 6.0), box=(4, 16), steps=100,
+                  desc="32^3 FP32, 2 dielectric boxes (eps_r 2-6), 100 steps"),
+}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class Dist:
+    """Barrier and max-reduction across ranks (torch.distributed; a no-op on one process)."""
+
+    def __init__(self, world: int, local: int):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch
+            import torch.distributed as td
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(local)
+            td.init_process_group(backend=backend)
+            self.td, self.torch = td, torch
+            self.dev = torch.device("cuda", local) if backend == "nccl" else torch.device("cpu")
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        t = self.torch.tensor([x], dtype=self.torch.float64, device=self.dev)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, throttle reasons)."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.lines: list[str] = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict | None:
+        if not self.proc:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                rows.append((float(parts[0]), float(parts[1]), parts[4:8]))
+            except ValueError:
+                continue
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, flags in rows for i, f in enumerate(flags) if f.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def hbm_peak():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        try:
+            return float(json.loads(f.read_text())["hbm_gbs"]), "measured"
+        except (KeyError, ValueError):
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def traffic_per_cell():
+    """DRAM bytes per cell update of the fused step kernel from the committed ncu summary, if any."""
+    f = ROOT / "profiles" / "yee_step_256.md"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("dram_bytes_per_cell_update:"):
+            try:
+                return float(line.split(":", 1)[1])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_sample(prob, shape, target_s: float = 10.0):
+    """Time the oracle (FP32 port of fdtd_cpu, all host threads) on a bounded sample of the workload."""
+    import oracle
+    import ptask_gb300 as P
+    f = P.zero_fields(*shape)
+    t0 = time.perf_counter()
+    oracle.step_ext_f32(f, 1, prob.params, prob.Ca, prob.Cb, prob.Da, prob.Db, prob.src, prob.wave)
+    one = time.perf_counter() - t0
+    steps = max(1, min(prob.wave.size or 1000, int(target_s / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    oracle.step_ext_f32(f, steps, prob.params, prob.Ca, prob.Cb, prob.Da, prob.Db, prob.src, prob.wave)
+    dt = time.perf_counter() - t0
+    cells = shape[0] * shape[1] * shape[2]
+    return {"value": cells * steps / dt / 1e6, "unit": "Mcell-updates/s", "cores": oracle.threads(),
+            "kind": "port",
+            "sample": f"{shape[0]}x{shape[1]}x{shape[2]} grid, first {steps} of the workload's time steps "
+                      f"({dt:.1f} s), oracle/fdtd_oracle.c FP32 with OpenMP"}
+
+
+def run_reference(args, wl, world, rank, local):
+    """--impl reference: the CPU implementation of the path on the host cores."""
+    if rank != 0:
+        return 0
+    import oracle
+    import ptask_gb300 as P
+    shape = wl["shape"]
+    prob = P.Problem.generate(*shape, n_boxes=wl["boxes"], eps=wl["eps"], box=wl["box"], steps=wl["steps"],
+                              source_mode=1, seed=2)
+    f = P.zero_fields(*shape)
+    t0 = time.perf_counter()
+    oracle.step_ext_f32(f, 1, prob.params, prob.Ca, prob.Cb, prob.Da, prob.Db, prob.src, prob.wave)
+    one = time.perf_counter() - t0
+    per = max(1, min(wl["steps"], int(2.0 / max(one, 1e-6))))   # ~2 s of CPU work per bench step
+    for _ in range(args.warmup):
+        oracle.step_ext_f32(f, 1, prob.params, prob.Ca, prob.Cb, prob.Da, prob.Db, prob.src, prob.wave)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.step_ext_f32(f, per, prob.params, prob.Ca, prob.Cb, prob.Da, prob.Db, prob.src, prob.wave)
+    dt = time.perf_counter() - t0
+    cells = shape[0] * shape[1] * shape[2]
+    value = cells * per * args.steps / dt / 1e6
+    sample = (f"{shape[0]}x{shape[1]}x{shape[2]} grid, {per} of the workload's {wl['steps']} time steps per "
+              f"bench step, oracle/fdtd_oracle.c FP32 port of fdtd_cpu with OpenMP")
+    line = {"metric": "FDTD Mcell-updates/s", "value": value, "unit": "Mcell-updates/s", "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": wl["desc"], "grid": list(shape), "time_steps": wl["steps"]},
+            "cpu_baseline": {"value": value, "unit": "Mcell-updates/s", "cores": oracle.threads(), "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "Mcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, wl, world, rank, local):
+    import ptask_gb300 as P
+    from ptask_gb300 import _lib
+    from ptask_gb300.device import DeviceBuffer, Event, HostBuffer
+
+    dist = Dist(world, local)
+    _lib.call("ptk_runtime_init", local)
+    shape = wl["shape"]
+    nx, ny, nz = shape
+    T = wl["steps"]
+    prob = P.Problem.generate(*shape, n_boxes=wl["boxes"], eps=wl["eps"], box=wl["box"], steps=T,
+                              source_mode=1, seed=2 + rank)
+    cells = nx * ny * nz
+    tiles = None
+    if not args.no_autotune:
+        tiles = P.tuned_tiles(nx, ny, nz) if hasattr(P, "tuned_tiles") else None
+
+    solver = P.Solver(prob.params)
+    if tiles:
+        solver.set_tiles(*tiles)
+    zero = P.zero_fields(*shape)
+    # Inputs resident in HBM: dense initial fields on the device, coefficients + source uploaded once.
+    dev_init = [DeviceBuffer.from_array(a) for a in zero]
+    solver.set_problem(prob)
+    ev0, ev1 = Event(), Event()
+    run_ev = [(Event(), Event()) for _ in range(args.steps)]
+
+    def device_step(k=None):
+        solver.set_fields_device([b.value for b in dev_init])
+        solver.reset_clock()
+        if k is not None:
+            run_ev[k][0].record()
+        solver.run(T)
+        if k is not None:
+            run_ev[k][1].record()
+
+    for _ in range(args.warmup):
+        device_step()
+    _lib.call("ptk_stream_sync", None)
+    dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    l0 = P.launch_count()
+    ev0.record()
+    for k in range(args.steps):
+        device_step(k)
+    ev1.record()
+    ev1.sync()
+    launches = P.launch_count() - l0
+    clk = clocks.stop()
+    dev_ms = ev0.elapsed_ms(ev1)
+    run_ms = [a.elapsed_ms(b) for a, b in run_ev]
+    dev_ms = dist.max(dev_ms)
+
+    # ---- end to end: pinned host buffers, H2D inputs + D2H results inside the timed region ----------
+    hin = [HostBuffer(a.shape) for a in zero]
+    for h, a in zip(hin, zero):
+        h.array[...] = a
+    hcoef = [HostBuffer(a.shape) for a in (prob.Ca, prob.Cb, prob.Da, prob.Db)]
+    for h, a in zip(hcoef, (prob.Ca, prob.Cb, prob.Da, prob.Db)):
+        h.array[...] = a
+    hwave = HostBuffer(prob.wave.shape)
+    hwave.array[...] = prob.wave
+    hout = [HostBuffer(a.shape) for a in zero]
+    import ctypes as C
+    V = C.c_void_p
+    in_ptrs = (V * 6)(*[h.ptr.value for h in hin])
+    out_ptrs = (V * 6)(*[h.ptr.value for h in hout])
+    h2d = sum(a.nbytes for a in zero) + 4 * prob.Ca.nbytes + prob.wave.nbytes
+    d2h = sum(a.nbytes for a in zero)
+
+    def e2e_step():
+        _lib.call("ptk_solver_set_fields", solver.handle, in_ptrs, P.PTK_HOST, None)
+        _lib.call("ptk_solver_set_coefficients", solver.handle, *[h.ptr.value for h in hcoef], P.PTK_HOST, None)
+        _lib.call("ptk_solver_set_source", solver.handle, *prob.src, hwave.ptr.value, prob.wave.size,
+                  P.PTK_HOST, None)
+        solver.reset_clock()
+        solver.run(T)
+        _lib.call("ptk_solver_get_fields", solver.handle, out_ptrs, P.PTK_HOST, None)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_s = dist.max(time.perf_counter() - t0)
+    result_ok = bool(np.isfinite(hout[5].array).all() and np.abs(hout[5].array).max() > 0)
+
+    total_cell_updates = cells * T * args.steps * world
+    value = total_cell_updates / (dev_ms / 1e3) / 1e6
+    e2e_value = total_cell_updates / e2e_s / 1e6
+    per_launch_ms = statistics.median(run_ms) / T
+    peak, peak_src = hbm_peak()
+    achieved = BYTES_PER_CELL * cells / (per_launch_ms / 1e3) / 1e9
+    tpc = traffic_per_cell()
+    by, kc = solver.tiles()
+    line = {
+        "metric": "FDTD Mcell-updates/s", "value": value, "unit": "Mcell-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded problem generator)",
+        "config": {"workload": wl["desc"], "grid": list(shape), "time_steps": T,
+                   "bench_step": "one complete solve (all time steps) from resident initial fields",
+                   "l2": "working set %.2f GB > 129 MB L2; no flush needed" % (16 * 4 * (nx + 1) * (ny + 1) * (nz + 1) / 1e9),
+                   "tiles": {"rows": by, "z_depth": kc}, "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_src,
+                     "traffic": (tpc * cells) if tpc else None,
+                     "kernel": "k_yee_step (fused H+E step)",
+                     "algorithmic_bytes_per_launch": BYTES_PER_CELL * cells,
+                     "launch_ms": per_launch_ms},
+        "e2e": {"value": e2e_value, "unit": "Mcell-updates/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3 / args.steps, "result_ok": result_ok},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_sample(prob, shape)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    solver.close()
+    dist.close()
+    return 0
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="plain256")
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_env()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, wl, world, rank, local)
+    return run_ours(args, wl, world, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,246 @@
+/*
+ * fdtd_oracle.c -- CPU oracle for the Yee-grid FDTD step of ptaskUnitTest/graphfdtd.cpp.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker, never the product: only tests/,
+ * __graft_entry__.smoke() and bench.py's cpu_baseline / --impl reference leg may load it.
+ * The shipped library (ptask_gb300) never links or calls anything here.
+ *
+ * What it restates (reference file:line, paths inside rossbach/ptask):
+ *   oracle_ref_f32      fdtd_cpu                    ptaskUnitTest/graphfdtd.cpp:314-340
+ *                       with the six field updates  graphfdtd.cpp:185-312
+ *                       (Hx 185-201, Hy 204-221, Hz 223-240, Ex 243-264, Ey 267-288, Ez 291-312)
+ *                       Scalar vacuum coefficients Dt/mu0 and Dt/eps0, FP32, same operation order,
+ *                       out-of-place update (the reference news a fresh array per update; here two
+ *                       buffers per field are swapped, which computes identical values).
+ *   oracle_ext_f32      the same scheme with per-cell coefficients (Ca, Cb for E, Da, Db for H) and
+ *                       a soft Ez point source added after the E update.  Not in the reference; it
+ *                       reduces bit-for-bit to oracle_ref_f32 when Ca=Da=1, Cb=fl(Dt/eps0),
+ *                       Db=fl(Dt/mu0) and the source is off (pinned by tests).
+ *   oracle_ext_f64      FP64 twin of oracle_ext_f32 (inputs widened once), for the "error vs FP64"
+ *                       figure.
+ *
+ * Layouts are the reference's (Simple3DArray.h:33): element (i,j,k) of an array with extents
+ * (d1,d2,d3) sits at i + j*d1 + k*d1*d2; the six fields have extents
+ *   Hx(Nx+1,Ny,Nz) Hy(Nx,Ny+1,Nz) Hz(Nx,Ny,Nz+1) Ex(Nx,Ny+1,Nz+1) Ey(Nx+1,Ny,Nz+1) Ez(Nx+1,Ny+1,Nz)
+ * (graphfdtd.cpp:68-86).  Coefficient arrays are per cell, extents (Nx,Ny,Nz); a field node outside
+ * the cell range (the i=Nx, j=Ny, k=Nz faces) uses the nearest cell (index clamped).
+ *
+ * Must be compiled with -ffp-contract=off so that no multiply-add is fused: every operation is
+ * rounded separately, as in the reference built for x86-64 SSE.  Loops over k are split across
+ * OpenMP threads when built with -fopenmp; each output element is computed independently, so the
+ * result is bit-identical for any thread count.
+ */
+#include <stdlib.h>
+#include <string.h>
+#include <stdint.h>
+
+typedef struct oracle_params {   /* same layout as FDTD_PARAMS, graphfdtd.h:6-19 */
+    int Nx, Ny, Nz;
+    float Cx, Cy, Cz, eps0, mu0, c0, Dt;
+} oracle_params;
+
+#define IDX(i, j, k, d1, d2) ((size_t)(i) + (size_t)(j) * (size_t)(d1) + (size_t)(k) * (size_t)(d1) * (size_t)(d2))
+
+static size_t field_count(int f, int Nx, int Ny, int Nz)
+{
+    switch (f) {
+    case 0: return (size_t)(Nx + 1) * Ny * Nz;          /* Hx */
+    case 1: return (size_t)Nx * (Ny + 1) * Nz;          /* Hy */
+    case 2: return (size_t)Nx * Ny * (Nz + 1);          /* Hz */
+    case 3: return (size_t)Nx * (Ny + 1) * (Nz + 1);    /* Ex */
+    case 4: return (size_t)(Nx + 1) * Ny * (Nz + 1);    /* Ey */
+    default: return (size_t)(Nx + 1) * (Ny + 1) * Nz;   /* Ez */
+    }
+}
+
+size_t oracle_field_count(int f, int Nx, int Ny, int Nz) { return field_count(f, Nx, Ny, Nz); }
+
+static inline int clampi(int v, int hi) { return v < hi ? v : hi - 1; }
+
+/* ------------------------------------------------------------------------------------------ */
+/* FP32 / FP64 generic body.  T is the arithmetic type; scalar coefficients are expressed as   */
+/* uniform arrays by the caller when coef == NULL (reference mode).                             */
+/* ------------------------------------------------------------------------------------------ */
+
+#define DEFINE_STEPPER(NAME, T)                                                                     \
+static void NAME(T *Hx, T *Hy, T *Hz, T *Ex, T *Ey, T *Ez,                                          \
+                 T *nHx, T *nHy, T *nHz, T *nEx, T *nEy, T *nEz,                                    \
+                 const T *Ca, const T *Cb, const T *Da, const T *Db,                                \
+                 T ca_s, T cb_s, T da_s, T db_s,                                                    \
+                 int Nx, int Ny, int Nz, T Cx, T Cy, T Cz,                                          \
+                 long src, T srcval)                                                                \
+{                                                                                                   \
+    /* ---- H half step: graphfdtd.cpp:185-240 (reads old E) ---- */                                \
+    int i, j, k;                                                                                    \
+    _Pragma("omp parallel for private(i, j) schedule(static)")                                      \
+    for (k = 0; k < Nz; ++k)                                                                        \
+        for (j = 0; j < Ny; ++j)                                                                    \
+            for (i = 0; i <= Nx; ++i) {                                                             \
+                size_t c = IDX(clampi(i, Nx), j, k, Nx, Ny);                                        \
+                T da = Da ? Da[c] : da_s, db = Db ? Db[c] : db_s;                                   \
+                T curl = (Ey[IDX(i, j, k + 1, Nx + 1, Ny)] - Ey[IDX(i, j, k, Nx + 1, Ny)]) * Cz     \
+                       - (Ez[IDX(i, j + 1, k, Nx + 1, Ny + 1)] - Ez[IDX(i, j, k, Nx + 1, Ny + 1)]) * Cy; \
+                size_t o = IDX(i, j, k, Nx + 1, Ny);                                                \
+                nHx[o] = da * Hx[o] + db * curl;                                                    \
+            }                                                                                       \
+    _Pragma("omp parallel for private(i, j) schedule(static)")                                      \
+    for (k = 0; k < Nz; ++k)                                                                        \
+        for (j = 0; j <= Ny; ++j)                                                                   \
+            for (i = 0; i < Nx; ++i) {                                                              \
+                size_t c = IDX(i, clampi(j, Ny), k, Nx, Ny);                                        \
+                T da = Da ? Da[c] : da_s, db = Db ? Db[c] : db_s;                                   \
+                T curl = (Ez[IDX(i + 1, j, k, Nx + 1, Ny + 1)] - Ez[IDX(i, j, k, Nx + 1, Ny + 1)]) * Cx \
+                       - (Ex[IDX(i, j, k + 1, Nx, Ny + 1)] - Ex[IDX(i, j, k, Nx, Ny + 1)]) * Cz;    \
+                size_t o = IDX(i, j, k, Nx, Ny + 1);                                                \
+                nHy[o] = da * Hy[o] + db * curl;                                                    \
+            }                                                                                       \
+    _Pragma("omp parallel for private(i, j) schedule(static)")                                      \
+    for (k = 0; k <= Nz; ++k)                                                                       \
+        for (j = 0; j < Ny; ++j)                                                                    \
+            for (i = 0; i < Nx; ++i) {                                                              \
+                size_t c = IDX(i, j, clampi(k, Nz), Nx, Ny);                                        \
+                T da = Da ? Da[c] : da_s, db = Db ? Db[c] : db_s;                                   \
+                T curl = (Ex[IDX(i, j + 1, k, Nx, Ny + 1)] - Ex[IDX(i, j, k, Nx, Ny + 1)]) * Cy     \
+                       - (Ey[IDX(i + 1, j, k, Nx + 1, Ny)] - Ey[IDX(i, j, k, Nx + 1, Ny)]) * Cx;    \
+                size_t o = IDX(i, j, k, Nx, Ny);                                                    \
+                nHz[o] = da * Hz[o] + db * curl;                                                    \
+            }                                                                                       \
+    /* ---- E half step: graphfdtd.cpp:243-312 (reads new H); faces copied ---- */                 \
+    _Pragma("omp parallel for private(i, j) schedule(static)")                                      \
+    for (k = 0; k <= Nz; ++k)                                                                       \
+        for (j = 0; j <= Ny; ++j)                                                                   \
+            for (i = 0; i < Nx; ++i) {                                                              \
+                size_t o = IDX(i, j, k, Nx, Ny + 1);                                                \
+                if (j < 1 || k < 1 || j > Ny - 1 || k > Nz - 1) { nEx[o] = Ex[o]; continue; }      \
+                size_t c = IDX(i, j, k, Nx, Ny);                                                    \
+                T ca = Ca ? Ca[c] : ca_s, cb = Cb ? Cb[c] : cb_s;                                   \
+                T curl = (nHz[IDX(i, j, k, Nx, Ny)] - nHz[IDX(i, j - 1, k, Nx, Ny)]) * Cy           \
+                       - (nHy[IDX(i, j, k, Nx, Ny + 1)] - nHy[IDX(i, j, k - 1, Nx, Ny + 1)]) * Cz;  \
+                nEx[o] = ca * Ex[o] + cb * curl;                                                    \
+            }                                                                                       \
+    _Pragma("omp parallel for private(i, j) schedule(static)")                                      \
+    for (k = 0; k <= Nz; ++k)                                                                       \
+        for (j = 0; j < Ny; ++j)                                                                    \
+            for (i = 0; i <= Nx; ++i) {                                                             \
+                size_t o = IDX(i, j, k, Nx + 1, Ny);                                                \
+                if (i < 1 || k < 1 || i > Nx - 1 || k > Nz - 1) { nEy[o] = Ey[o]; continue; }      \
+                size_t c = IDX(i, j, k, Nx, Ny);                                                    \
+                T ca = Ca ? Ca[c] : ca_s, cb = Cb ? Cb[c] : cb_s;                                   \
+                T curl = (nHx[IDX(i, j, k, Nx + 1, Ny)] - nHx[IDX(i, j, k - 1, Nx + 1, Ny)]) * Cz   \
+                       - (nHz[IDX(i, j, k, Nx, Ny)] - nHz[IDX(i - 1, j, k, Nx, Ny)]) * Cx;          \
+                nEy[o] = ca * Ey[o] + cb * curl;                                                    \
+            }                                                                                       \
+    _Pragma("omp parallel for private(i, j) schedule(static)")                                      \
+    for (k = 0; k < Nz; ++k)                                                                        \
+        for (j = 0; j <= Ny; ++j)                                                                   \
+            for (i = 0; i <= Nx; ++i) {                                                             \
+                size_t o = IDX(i, j, k, Nx + 1, Ny + 1);                                            \
+                if (i < 1 || j < 1 || i > Nx - 1 || j > Ny - 1) { nEz[o] = Ez[o]; continue; }      \
+                size_t c = IDX(i, j, k, Nx, Ny);                                                    \
+                T ca = Ca ? Ca[c] : ca_s, cb = Cb ? Cb[c] : cb_s;                                   \
+                T curl = (nHy[IDX(i, j, k, Nx, Ny + 1)] - nHy[IDX(i - 1, j, k, Nx, Ny + 1)]) * Cx   \
+                       - (nHx[IDX(i, j, k, Nx + 1, Ny)] - nHx[IDX(i, j - 1, k, Nx + 1, Ny)]) * Cy;  \
+                nEz[o] = ca * Ez[o] + cb * curl;                                                    \
+            }                                                                                       \
+    if (src >= 0) nEz[src] = nEz[src] + srcval;                                                     \
+}
+
+DEFINE_STEPPER(step_f32, float)
+DEFINE_STEPPER(step_f64, double)
+
+/* Swap the caller's six arrays through scratch copies for T steps.  The arrays are updated in
+ * place: on return they hold the fields after T steps. */
+#define DEFINE_DRIVER(NAME, T, STEP)                                                                \
+static int NAME(T *f[6], const T *Ca, const T *Cb, const T *Da, const T *Db,                        \
+                T ca_s, T cb_s, T da_s, T db_s, int Nx, int Ny, int Nz, T Cx, T Cy, T Cz,           \
+                int steps, int si, int sj, int sk, const float *wave, int nwave)                    \
+{                                                                                                   \
+    T *g[6];                                                                                        \
+    int q, n;                                                                                       \
+    long src = -1;                                                                                  \
+    if (Nx < 1 || Ny < 1 || Nz < 1 || steps < 0) return 1;                                          \
+    if (wave && si >= 0) src = (long)IDX(si, sj, sk, Nx + 1, Ny + 1);                               \
+    for (q = 0; q < 6; ++q) {                                                                       \
+        g[q] = (T *)malloc(field_count(q, Nx, Ny, Nz) * sizeof(T));                                 \
+        if (!g[q]) { while (q--) free(g[q]); return 2; }                                            \
+    }                                                                                               \
+    for (n = 0; n < steps; ++n) {                                                                   \
+        T sv = (src >= 0 && n < nwave) ? (T)wave[n] : (T)0;                                         \
+        STEP(f[0], f[1], f[2], f[3], f[4], f[5], g[0], g[1], g[2], g[3], g[4], g[5],                \
+             Ca, Cb, Da, Db, ca_s, cb_s, da_s, db_s, Nx, Ny, Nz, Cx, Cy, Cz,                        \
+             (src >= 0 && n < nwave) ? src : -1, sv);                                               \
+        for (q = 0; q < 6; ++q) { T *t = f[q]; f[q] = g[q]; g[q] = t; }                             \
+    }                                                                                               \
+    /* after an odd number of swaps the results live in the scratch arrays: copy back */            \
+    if (steps & 1)                                                                                  \
+        for (q = 0; q < 6; ++q) {                                                                   \
+            memcpy(g[q], f[q], field_count(q, Nx, Ny, Nz) * sizeof(T));                             \
+            T *t = f[q]; f[q] = g[q]; g[q] = t;                                                     \
+        }                                                                                           \
+    for (q = 0; q < 6; ++q) free(g[q]);                                                             \
+    return 0;                                                                                       \
+}
+
+DEFINE_DRIVER(drive_f32, float, step_f32)
+DEFINE_DRIVER(drive_f64, double, step_f64)
+
+/* Reference mode: fdtd_cpu (graphfdtd.cpp:314-340) on the six arrays in place. */
+int oracle_ref_f32(float *Hx, float *Hy, float *Hz, float *Ex, float *Ey, float *Ez,
+                   int steps, const oracle_params *p)
+{
+    float *f[6] = {Hx, Hy, Hz, Ex, Ey, Ez};
+    float ch = p->Dt / p->mu0;     /* (params.Dt/params.mu0), graphfdtd.cpp:198 */
+    float ce = p->Dt / p->eps0;    /* (params.Dt/params.eps0), graphfdtd.cpp:260 */
+    return drive_f32(f, NULL, NULL, NULL, NULL, 1.0f, ce, 1.0f, ch, p->Nx, p->Ny, p->Nz,
+                     p->Cx, p->Cy, p->Cz, steps, -1, 0, 0, NULL, 0);
+}
+
+/* Extended mode, FP32: per-cell coefficients and an optional soft Ez source at (si,sj,sk)
+ * (si < 0 disables it); wave[n] is added to Ez after the E update of step n. */
+int oracle_ext_f32(float *Hx, float *Hy, float *Hz, float *Ex, float *Ey, float *Ez,
+                   const float *Ca, const float *Cb, const float *Da, const float *Db,
+                   int steps, const oracle_params *p, int si, int sj, int sk,
+                   const float *wave, int nwave)
+{
+    float *f[6] = {Hx, Hy, Hz, Ex, Ey, Ez};
+    return drive_f32(f, Ca, Cb, Da, Db, 0, 0, 0, 0, p->Nx, p->Ny, p->Nz, p->Cx, p->Cy, p->Cz,
+                     steps, si, sj, sk, wave, nwave);
+}
+
+/* Extended mode, FP64: FP32 inputs are widened once; results are written to the double arrays
+ * out[0..5] (which need not be initialised). */
+int oracle_ext_f64(const float *const in[6], double *const out[6],
+                   const float *Ca, const float *Cb, const float *Da, const float *Db,
+                   int steps, const oracle_params *p, int si, int sj, int sk,
+                   const float *wave, int nwave)
+{
+    int Nx = p->Nx, Ny = p->Ny, Nz = p->Nz, q, rc;
+    size_t ncell = (size_t)Nx * Ny * Nz, n;
+    double *f[6], *c[4] = {0, 0, 0, 0};
+    const float *cs[4] = {Ca, Cb, Da, Db};
+    for (q = 0; q < 6; ++q) {
+        size_t m = field_count(q, Nx, Ny, Nz);
+        f[q] = out[q];
+        for (n = 0; n < m; ++n) f[q][n] = (double)in[q][n];
+    }
+    for (q = 0; q < 4; ++q) {
+        c[q] = (double *)malloc(ncell * sizeof(double));
+        if (!c[q]) { while (q--) free(c[q]); return 2; }
+        for (n = 0; n < ncell; ++n) c[q][n] = (double)cs[q][n];
+    }
+    rc = drive_f64(f, c[0], c[1], c[2], c[3], 0, 0, 0, 0, Nx, Ny, Nz, (double)p->Cx,
+                   (double)p->Cy, (double)p->Cz, steps, si, sj, sk, wave, nwave);
+    for (q = 0; q < 4; ++q) free(c[q]);
+    return rc;
+}
+
+/* Threads the OpenMP runtime will use (1 when built without OpenMP). */
+int oracle_threads(void)
+{
+#ifdef _OPENMP
+    extern int omp_get_max_threads(void);
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}

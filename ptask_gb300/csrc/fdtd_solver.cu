@@ -1,0 +1,573 @@
+// fdtd_solver.cu -- device-resident FDTD instance with CUDA-graph replay of the fused step.
+//
+// A solver owns, in HBM: two buffers of each of the six fields (ping-pong), the four coefficient
+// arrays, the source waveform and a one-entry work list (InstDesc + tile prefix).  A run of T steps
+// replays a captured graph of L fused-step launches followed by one "advance" launch that moves the
+// instance's step counter, so the only host work per L steps is one cudaGraphLaunch.  This is the
+// scheduler's execution of an iterated FDTD cycle: the per-task dispatch of the reference
+// (ptask/task.cpp:3822-3900 -> ptask/cutask.cpp:634-705, six launches per step with host-side
+// readiness checks) becomes one replayed graph.
+#include "ptk_internal.h"
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
+namespace ptk {
+
+__global__ void k_store_desc(InstDesc *dst, InstDesc v) { *dst = v; }
+
+__global__ void k_store_tile0(int *dst, int a, int b)
+{
+    dst[0] = a;
+    dst[1] = b;
+}
+
+static int store_desc(InstDesc *d_dst, const InstDesc &v, cudaStream_t s)
+{
+    k_store_desc<<<1, 1, 0, s>>>(d_dst, v);
+    PTK_CUDA_TRY(cudaGetLastError());
+    count_launches(1);
+    return PTK_OK;
+}
+
+// Default tile shape: rows of 8, z depth chosen so the grid holds several waves of CTAs.
+static void default_tiles(int nx, int ny, int nz, int *by, int *kc)
+{
+    *by = 8;
+    const long long cols = (long long)((nx + kTileX - 1) / kTileX) * ((ny + 7) / 8);
+    const long long want = 4LL * std::max(1, sm_count()) * 2;   // ~4 waves at 2 CTAs per SM
+    long long zc = (want + cols - 1) / std::max(1LL, cols);
+    int k = (int)((nz + zc - 1) / std::max(1LL, zc));
+    if (k < 16) k = 16;
+    if (k >= nz) k = 0;
+    *kc = k;
+}
+
+struct GraphKey {
+    int len, by, kc;
+    bool operator<(const GraphKey &o) const
+    {
+        return std::tie(len, by, kc) < std::tie(o.len, o.by, o.kc);
+    }
+};
+
+}  // namespace ptk
+
+using namespace ptk;
+
+struct ptk_solver {
+    ptk_fdtd_params p;
+    Layout L;
+    float *buf[2][6] = {};
+    float *coef[4] = {};
+    float *wave = nullptr;
+    int nwave = 0;
+    long long src = -1;
+    int step = 0;              // host mirror of the device step counter
+    int by = 0, kc = 0;
+    int total_tiles = 0;
+    InstDesc *d_desc = nullptr;
+    int *d_tile0 = nullptr;
+    cudaStream_t cap = nullptr;   // capture stream
+    std::map<GraphKey, cudaGraphExec_t> graphs;
+    long long last_launches = 0;
+    std::mutex mu;
+};
+
+namespace ptk {
+
+static InstDesc host_desc(const ptk_solver *s, int steps_left)
+{
+    InstDesc d{};
+    for (int b = 0; b < 2; ++b)
+        for (int f = 0; f < 6; ++f) d.buf[b][f] = s->buf[b][f];
+    for (int c = 0; c < 4; ++c) d.coef[c] = s->coef[c];
+    d.wave = s->wave;
+    d.plane = s->L.plane;
+    d.nx = s->L.nx; d.ny = s->L.ny; d.nz = s->L.nz; d.pitch = s->L.pitch;
+    d.cx = s->p.Cx; d.cy = s->p.Cy; d.cz = s->p.Cz;
+    d.src = s->nwave > 0 ? s->src : -1;
+    d.nwave = s->nwave;
+    d.step = s->step;
+    d.steps_left = steps_left;
+    plan_tiles(d, s->by, s->kc);
+    return d;
+}
+
+static int solver_sync_desc(ptk_solver *s, int steps_left, cudaStream_t st)
+{
+    InstDesc d = host_desc(s, steps_left);
+    s->total_tiles = d.tiles_x * d.tiles_y * d.tiles_z + d.face_tiles;
+    int rc = store_desc(s->d_desc, d, st);
+    if (rc) return rc;
+    k_store_tile0<<<1, 1, 0, st>>>(s->d_tile0, 0, s->total_tiles);
+    PTK_CUDA_TRY(cudaGetLastError());
+    count_launches(1);
+    return PTK_OK;
+}
+
+static void drop_graphs(ptk_solver *s)
+{
+    for (auto &kv : s->graphs) cudaGraphExecDestroy(kv.second);
+    s->graphs.clear();
+}
+
+// Graph of `len` fused steps + one advance for this solver's current tile shape.
+static int solver_graph(ptk_solver *s, int len, cudaGraphExec_t *out)
+{
+    GraphKey key{len, s->by, s->kc};
+    auto it = s->graphs.find(key);
+    if (it != s->graphs.end()) {
+        *out = it->second;
+        return PTK_OK;
+    }
+    if (!s->cap) PTK_CUDA_TRY(cudaStreamCreateWithFlags(&s->cap, cudaStreamNonBlocking));
+    PTK_CUDA_TRY(cudaStreamBeginCapture(s->cap, cudaStreamCaptureModeThreadLocal));
+    set_capturing(true);
+    int rc = PTK_OK;
+    for (int q = 0; q < len && rc == PTK_OK; ++q)
+        rc = launch_yee_step(s->d_desc, s->d_tile0, 1, s->total_tiles, q, s->by, s->cap);
+    if (rc == PTK_OK) rc = launch_advance(s->d_desc, 1, len, s->cap);
+    set_capturing(false);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s->cap, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return set_error(PTK_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+    cudaGraphExec_t ex = nullptr;
+    e = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return set_error(PTK_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+    s->graphs[key] = ex;
+    *out = ex;
+    return PTK_OK;
+}
+
+static constexpr int kChunk = 32;   // fused steps per replayed graph
+
+int solver_run(ptk_solver *s, int steps, cudaStream_t st)
+{
+    if (steps < 0) return set_error(PTK_ERR_INVALID, "negative step count");
+    s->last_launches = 0;
+    if (steps == 0) return PTK_OK;
+    int rc = solver_sync_desc(s, steps, st);
+    if (rc) return rc;
+    int left = steps;
+    while (left > 0) {
+        const int len = left >= kChunk ? kChunk : left;
+        cudaGraphExec_t ex;
+        rc = solver_graph(s, len, &ex);
+        if (rc) return rc;
+        PTK_CUDA_TRY(cudaGraphLaunch(ex, st));
+        count_graph_launch(len + 1);
+        s->last_launches += len + 1;
+        left -= len;
+    }
+    s->step += steps;
+    return PTK_OK;
+}
+
+static size_t field_bytes(int f, const ptk_fdtd_params &p)
+{
+    int ex, ey, ez;
+    field_extents(f, p.Nx, p.Ny, p.Nz, &ex, &ey, &ez);
+    return (size_t)ex * ey * ez * sizeof(float);
+}
+
+}  // namespace ptk
+
+static inline cudaStream_t S(void *s) { return s ? (cudaStream_t)s : default_stream(); }
+
+static int validate_params(const ptk_fdtd_params *p)
+{
+    PTK_CHECK_ARG(p, "params is NULL");
+    PTK_CHECK_ARG(p->Nx >= 1 && p->Ny >= 1 && p->Nz >= 1, "grid %dx%dx%d must be at least 1x1x1",
+                  p->Nx, p->Ny, p->Nz);
+    PTK_CHECK_ARG((long long)p->Nx * p->Ny * p->Nz <= (1LL << 33), "grid too large");
+    return PTK_OK;
+}
+
+extern "C" {
+
+int ptk_solver_create(const ptk_fdtd_params *p, ptk_solver **out)
+{
+    clear_error();
+    int rc = validate_params(p);
+    if (rc) return rc;
+    PTK_CHECK_ARG(out, "out is NULL");
+    rc = ensure_init();
+    if (rc) return rc;
+    ptk_solver *s = new ptk_solver();
+    s->p = *p;
+    s->L = make_layout(p->Nx, p->Ny, p->Nz);
+    default_tiles(p->Nx, p->Ny, p->Nz, &s->by, &s->kc);
+    cudaStream_t st = default_stream();
+    const size_t bytes = (size_t)s->L.total * sizeof(float);
+    for (int b = 0; b < 2 && rc == PTK_OK; ++b)
+        for (int f = 0; f < 6 && rc == PTK_OK; ++f) rc = pool_alloc(bytes, st, (void **)&s->buf[b][f]);
+    for (int c = 0; c < 4 && rc == PTK_OK; ++c) rc = pool_alloc(bytes, st, (void **)&s->coef[c]);
+    if (rc == PTK_OK) rc = pool_alloc(sizeof(InstDesc), st, (void **)&s->d_desc);
+    if (rc == PTK_OK) rc = pool_alloc(2 * sizeof(int), st, (void **)&s->d_tile0);
+    if (rc) {
+        ptk_solver_destroy(s);
+        return rc;
+    }
+    for (int b = 0; b < 2; ++b)
+        for (int f = 0; f < 6; ++f) cudaMemsetAsync(s->buf[b][f], 0, bytes, st);
+    for (int c = 0; c < 4; ++c) cudaMemsetAsync(s->coef[c], 0, bytes, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) {
+        ptk_solver_destroy(s);
+        return set_error(PTK_ERR_CUDA, "solver initialisation failed");
+    }
+    rc = ptk_solver_set_vacuum(s, nullptr);
+    if (rc) {
+        ptk_solver_destroy(s);
+        return rc;
+    }
+    *out = s;
+    return PTK_OK;
+}
+
+int ptk_solver_destroy(ptk_solver *s)
+{
+    if (!s) return PTK_OK;
+    cudaStream_t st = default_stream();
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        drop_graphs(s);
+        for (int b = 0; b < 2; ++b)
+            for (int f = 0; f < 6; ++f) pool_free(s->buf[b][f], st);
+        for (int c = 0; c < 4; ++c) pool_free(s->coef[c], st);
+        pool_free(s->wave, st);
+        pool_free(s->d_desc, st);
+        pool_free(s->d_tile0, st);
+        if (s->cap) cudaStreamDestroy(s->cap);
+    }
+    cudaStreamSynchronize(st);
+    delete s;
+    return PTK_OK;
+}
+
+int ptk_solver_set_fields(ptk_solver *s, const float *const f[6], int where, void *stream)
+{
+    clear_error();
+    PTK_CHECK_ARG(s && f, "NULL argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    cudaStream_t st = S(stream);
+    for (int q = 0; q < 6; ++q) {
+        PTK_CHECK_ARG(f[q], "field %d is NULL", q);
+        int ex, ey, ez;
+        field_extents(q, s->p.Nx, s->p.Ny, s->p.Nz, &ex, &ey, &ez);
+        const float *src = f[q];
+        float *stage = nullptr;
+        if (where == PTK_HOST) {
+            int rc = pool_alloc(field_bytes(q, s->p), st, (void **)&stage);
+            if (rc) return rc;
+            PTK_CUDA_TRY(cudaMemcpyAsync(stage, f[q], field_bytes(q, s->p), cudaMemcpyHostToDevice, st));
+            src = stage;
+        }
+        int rc = launch_pack_field(src, ex, ey, ez, s->L, s->buf[0][q], s->buf[1][q], st);
+        if (stage) pool_free(stage, st);
+        if (rc) return rc;
+    }
+    return PTK_OK;
+}
+
+int ptk_solver_get_fields(ptk_solver *s, float *const f[6], int where, void *stream)
+{
+    clear_error();
+    PTK_CHECK_ARG(s && f, "NULL argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    cudaStream_t st = S(stream);
+    const int par = s->step & 1;
+    for (int q = 0; q < 6; ++q) {
+        PTK_CHECK_ARG(f[q], "field %d is NULL", q);
+        int ex, ey, ez;
+        field_extents(q, s->p.Nx, s->p.Ny, s->p.Nz, &ex, &ey, &ez);
+        float *dst = f[q];
+        float *stage = nullptr;
+        if (where == PTK_HOST) {
+            int rc = pool_alloc(field_bytes(q, s->p), st, (void **)&stage);
+            if (rc) return rc;
+            dst = stage;
+        }
+        int rc = launch_unpack_field(s->buf[par][q], ex, ey, ez, s->L, dst, st);
+        if (rc) return rc;
+        if (stage) {
+            PTK_CUDA_TRY(cudaMemcpyAsync(f[q], stage, field_bytes(q, s->p), cudaMemcpyDeviceToHost, st));
+            pool_free(stage, st);
+        }
+    }
+    if (where == PTK_HOST) PTK_CUDA_TRY(cudaStreamSynchronize(st));
+    return PTK_OK;
+}
+
+int ptk_solver_set_coefficients(ptk_solver *s, const float *Ca, const float *Cb, const float *Da,
+                                const float *Db, int where, void *stream)
+{
+    clear_error();
+    PTK_CHECK_ARG(s && Ca && Cb && Da && Db, "NULL argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    cudaStream_t st = S(stream);
+    const float *src[4] = {Ca, Cb, Da, Db};
+    const size_t bytes = (size_t)s->p.Nx * s->p.Ny * s->p.Nz * sizeof(float);
+    for (int c = 0; c < 4; ++c) {
+        const float *a = src[c];
+        float *stage = nullptr;
+        if (where == PTK_HOST) {
+            int rc = pool_alloc(bytes, st, (void **)&stage);
+            if (rc) return rc;
+            PTK_CUDA_TRY(cudaMemcpyAsync(stage, src[c], bytes, cudaMemcpyHostToDevice, st));
+            a = stage;
+        }
+        int rc = launch_pack_coef(a, s->L, s->coef[c], st);
+        if (stage) pool_free(stage, st);
+        if (rc) return rc;
+    }
+    return PTK_OK;
+}
+
+int ptk_solver_set_vacuum(ptk_solver *s, void *stream)
+{
+    PTK_CHECK_ARG(s, "NULL solver");
+    cudaStream_t st = S(stream);
+    // Scalar coefficients of the reference: (params.Dt/params.eps0), (params.Dt/params.mu0) in FP32.
+    const float ce = s->p.Dt / s->p.eps0;
+    const float ch = s->p.Dt / s->p.mu0;
+    const float v[4] = {1.0f, ce, 1.0f, ch};
+    for (int c = 0; c < 4; ++c) {
+        int rc = launch_fill(s->coef[c], s->L.total, v[c], st);
+        if (rc) return rc;
+    }
+    return PTK_OK;
+}
+
+int ptk_solver_set_source(ptk_solver *s, int i, int j, int k, const float *wave, int nwave, int where,
+                          void *stream)
+{
+    clear_error();
+    PTK_CHECK_ARG(s, "NULL solver");
+    std::lock_guard<std::mutex> lk(s->mu);
+    cudaStream_t st = S(stream);
+    if (nwave <= 0 || !wave) {
+        s->nwave = 0;
+        s->src = -1;
+        return PTK_OK;
+    }
+    PTK_CHECK_ARG(i >= 1 && i < s->p.Nx && j >= 1 && j < s->p.Ny && k >= 0 && k < s->p.Nz,
+                  "source node (%d,%d,%d) must be an interior Ez node of a %dx%dx%d grid", i, j, k,
+                  s->p.Nx, s->p.Ny, s->p.Nz);
+    if (s->wave) pool_free(s->wave, st);
+    s->wave = nullptr;
+    int rc = pool_alloc((size_t)nwave * sizeof(float), st, (void **)&s->wave);
+    if (rc) return rc;
+    PTK_CUDA_TRY(cudaMemcpyAsync(s->wave, wave, (size_t)nwave * sizeof(float),
+                                 where == PTK_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, st));
+    s->nwave = nwave;
+    s->src = (long long)i + (long long)s->L.pitch * j + s->L.plane * k;
+    return PTK_OK;
+}
+
+int ptk_solver_reset_clock(ptk_solver *s, void *stream)
+{
+    PTK_CHECK_ARG(s, "NULL solver");
+    (void)stream;
+    std::lock_guard<std::mutex> lk(s->mu);
+    // The parity of the current field buffer is tied to the step counter; keep it and only
+    // rebase the waveform index by storing the offset in the host mirror.
+    if (s->step & 1) {
+        // Swap buffer roles so that step 0 reads the buffer that holds the current fields.
+        for (int f = 0; f < 6; ++f) std::swap(s->buf[0][f], s->buf[1][f]);
+    }
+    s->step = 0;
+    return PTK_OK;
+}
+
+int ptk_solver_set_tiles(ptk_solver *s, const ptk_tile_config *cfg)
+{
+    PTK_CHECK_ARG(s && cfg, "NULL argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    int by = cfg->by, kc = cfg->kc;
+    if (by == 0 && kc == 0) {
+        default_tiles(s->p.Nx, s->p.Ny, s->p.Nz, &by, &kc);
+    }
+    PTK_CHECK_ARG(by == 4 || by == 8 || by == 16, "tile rows must be 4, 8 or 16 (got %d)", by);
+    PTK_CHECK_ARG(kc >= 0, "tile depth must be >= 0");
+    if (kc >= s->p.Nz) kc = 0;
+    if (by != s->by || kc != s->kc) {
+        s->by = by;
+        s->kc = kc;
+    }
+    return PTK_OK;
+}
+
+int ptk_solver_get_tiles(const ptk_solver *s, ptk_tile_config *cfg)
+{
+    PTK_CHECK_ARG(s && cfg, "NULL argument");
+    cfg->by = s->by;
+    cfg->kc = s->kc;
+    return PTK_OK;
+}
+
+int ptk_solver_run(ptk_solver *s, int steps, void *stream)
+{
+    clear_error();
+    PTK_CHECK_ARG(s, "NULL solver");
+    std::lock_guard<std::mutex> lk(s->mu);
+    return solver_run(s, steps, S(stream));
+}
+
+int ptk_solver_bytes(const ptk_solver *s, size_t *bytes)
+{
+    PTK_CHECK_ARG(s && bytes, "NULL argument");
+    *bytes = (size_t)s->L.total * sizeof(float) * 16 + (size_t)s->nwave * sizeof(float);
+    return PTK_OK;
+}
+
+int ptk_solver_last_launches(const ptk_solver *s, long long *launches)
+{
+    PTK_CHECK_ARG(s && launches, "NULL argument");
+    *launches = s->last_launches;
+    return PTK_OK;
+}
+
+int ptk_fdtd_solve(const ptk_fdtd_params *p, float *const fields[6], const float *Ca, const float *Cb,
+                   const float *Da, const float *Db, int si, int sj, int sk, const float *wave,
+                   int nwave, int steps, float *ms)
+{
+    clear_error();
+    ptk_solver *s = nullptr;
+    int rc = ptk_solver_create(p, &s);
+    if (rc) return rc;
+    cudaStream_t st = default_stream();
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    rc = ptk_solver_set_fields(s, fields, PTK_HOST, st);
+    if (!rc && Ca) rc = ptk_solver_set_coefficients(s, Ca, Cb, Da, Db, PTK_HOST, st);
+    if (!rc && wave && nwave > 0) rc = ptk_solver_set_source(s, si, sj, sk, wave, nwave, PTK_HOST, st);
+    if (!rc) rc = ptk_solver_run(s, steps, st);
+    if (!rc) rc = ptk_solver_get_fields(s, fields, PTK_HOST, st);
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
+    if (ms) cudaEventElapsedTime(ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ptk_solver_destroy(s);
+    return rc;
+}
+
+int ptk_launch_field_update(int field, const float *in0, const float *in1, const float *in2,
+                            const ptk_fdtd_params *p, float *out, void *stream)
+{
+    clear_error();
+    int rc = validate_params(p);
+    if (rc) return rc;
+    PTK_CHECK_ARG(field >= 0 && field < 6, "field id %d out of range", field);
+    PTK_CHECK_ARG(in0 && in1 && in2 && out, "NULL buffer");
+    rc = ensure_init();
+    if (rc) return rc;
+    return launch_field_ref(field, in0, in1, in2, *p, out, S(stream));
+}
+
+int ptk_launch_h_half_step(const float *const in[6], float *const out_h[3], const ptk_fdtd_params *p,
+                           void *stream)
+{
+    clear_error();
+    int rc = validate_params(p);
+    if (rc) return rc;
+    PTK_CHECK_ARG(in && out_h, "NULL buffer");
+    rc = ensure_init();
+    if (rc) return rc;
+    return launch_h_half(in, out_h, *p, S(stream));
+}
+
+int ptk_launch_e_half_step(const float *const e_in[3], const float *const h_new[3],
+                           float *const out_e[3], const ptk_fdtd_params *p, void *stream)
+{
+    clear_error();
+    int rc = validate_params(p);
+    if (rc) return rc;
+    PTK_CHECK_ARG(e_in && h_new && out_e, "NULL buffer");
+    rc = ensure_init();
+    if (rc) return rc;
+    return launch_e_half(e_in, h_new, out_e, *p, S(stream));
+}
+
+// --------------------------------------------------------------------------------------------
+// Autotuner: time candidate (rows, depth) shapes on a scratch solver of the requested size.
+// --------------------------------------------------------------------------------------------
+static std::mutex g_tune_mu;
+static std::map<std::tuple<int, int, int>, std::pair<ptk_tile_config, float>> g_tune_cache;
+
+int ptk_autotune_tiles(int Nx, int Ny, int Nz, ptk_tile_config *best, float *best_ms)
+{
+    clear_error();
+    PTK_CHECK_ARG(best, "NULL argument");
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find({Nx, Ny, Nz});
+        if (it != g_tune_cache.end()) {
+            *best = it->second.first;
+            if (best_ms) *best_ms = it->second.second;
+            return PTK_OK;
+        }
+    }
+    ptk_fdtd_params p{};
+    int rc = ptk_reference_params(Nx, Ny, Nz, &p);
+    if (rc) return rc;
+    ptk_solver *s = nullptr;
+    rc = ptk_solver_create(&p, &s);
+    if (rc) return rc;
+    cudaStream_t st = default_stream();
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int rows[3] = {4, 8, 16};
+    const int depths[6] = {8, 16, 32, 64, 128, 0};
+    const long long cells = (long long)Nx * Ny * Nz;
+    const int steps = (int)std::max(4LL, std::min(64LL, 400000000LL / std::max(1LL, cells)));
+    float best_t = 1e30f;
+    ptk_tile_config bc{8, 0};
+    for (int by : rows) {
+        for (int kc : depths) {
+            if (kc != 0 && kc >= Nz) continue;
+            ptk_tile_config c{by, kc};
+            if (ptk_solver_set_tiles(s, &c)) continue;
+            if (ptk_solver_run(s, 2, st)) { rc = PTK_ERR_CUDA; break; }
+            cudaEventRecord(e0, st);
+            if (ptk_solver_run(s, steps, st)) { rc = PTK_ERR_CUDA; break; }
+            cudaEventRecord(e1, st);
+            cudaEventSynchronize(e1);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            ms /= steps;
+            if (ms < best_t) {
+                best_t = ms;
+                bc = c;
+            }
+        }
+        if (rc) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ptk_solver_destroy(s);
+    if (rc) return rc;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_cache[{Nx, Ny, Nz}] = {bc, best_t};
+    }
+    *best = bc;
+    if (best_ms) *best_ms = best_t;
+    return PTK_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,109 @@
+// ptk_internal.h -- declarations shared by the CUDA translation units of libptask_gb300.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include "../../include/ptask_gb300.h"
+
+namespace ptk {
+
+// ---------------------------------------------------------------------------------------------
+// Error reporting: every C entry point funnels failures through set_error, which stores a
+// thread-local message for ptk_last_error() and returns the code.
+// ---------------------------------------------------------------------------------------------
+int set_error(int code, const char *fmt, ...);
+void clear_error();
+
+#define PTK_CUDA_TRY(expr)                                                                        \
+    do {                                                                                          \
+        cudaError_t _e = (expr);                                                                  \
+        if (_e != cudaSuccess)                                                                    \
+            return ::ptk::set_error(PTK_ERR_CUDA, "%s failed: %s (%s:%d)", #expr,                 \
+                                    cudaGetErrorString(_e), __FILE__, __LINE__);                  \
+    } while (0)
+
+#define PTK_CHECK_ARG(cond, ...)                                                                  \
+    do {                                                                                          \
+        if (!(cond)) return ::ptk::set_error(PTK_ERR_INVALID, __VA_ARGS__);                      \
+    } while (0)
+
+// Ensure the runtime is initialised on the current thread (device selected).
+int ensure_init();
+cudaStream_t default_stream();
+int sm_count();
+
+// Stream-ordered device pool (BlockPool replacement).
+int pool_alloc(size_t bytes, cudaStream_t s, void **p);
+int pool_free(void *p, cudaStream_t s);
+
+// ---------------------------------------------------------------------------------------------
+// Padded HBM layout of one FDTD instance.
+//   node (i,j,k), 0<=i<=Nx, 0<=j<=Ny, 0<=k<=Nz, lives at i + pitch*j + plane*k with
+//   pitch = roundup(Nx+1, 32) floats (rows start on 128-byte boundaries) and plane = pitch*(Ny+1).
+// All six fields and the four coefficient arrays share this indexing, so one offset addresses
+// every operand of a cell.  Fields are double-buffered (ping-pong); E nodes on the PEC walls are
+// never rewritten with new values, so both buffers keep them from the upload onwards.
+// ---------------------------------------------------------------------------------------------
+struct Layout {
+    int nx, ny, nz;
+    int pitch;
+    long long plane;
+    long long total;   // floats per array (plane * (nz+1))
+};
+Layout make_layout(int nx, int ny, int nz);
+
+// Device-side descriptor of one instance, read by the step kernel.
+struct InstDesc {
+    float *buf[2][6];          // ping-pong fields: Hx Hy Hz Ex Ey Ez
+    const float *coef[4];      // Ca Cb Da Db (padded, face nodes replicate the nearest cell)
+    const float *wave;         // source waveform, indexed by absolute step
+    long long plane;
+    int nx, ny, nz, pitch;
+    float cx, cy, cz;
+    long long src;             // padded index of the Ez source node, -1 = none
+    int nwave;
+    int step;                  // absolute index of the first step of the current chunk
+    int steps_left;            // steps still to run at the start of the current chunk
+    int tiles_x, tiles_y, tiles_z, face_tiles;
+    int kc;                    // z-planes per main tile
+    int pad_;
+};
+
+// Shape of the fused step kernel's main tiles (x width is fixed at 128 cells).
+constexpr int kTileX = 128;
+constexpr int kFaceCellsPerThread = 4;
+
+// Work-list geometry for an instance under tile rows `by` and depth `kc`.
+void plan_tiles(InstDesc &d, int by, int kc);
+int face_tile_cells(int by);
+
+// Launchers (asynchronous on `s`).
+int launch_yee_step(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles,
+                    int s_offset, int by, cudaStream_t s);
+int launch_advance(InstDesc *d_insts, int ninst, int nsteps, cudaStream_t s);
+int launch_pack_field(const float *src, int ex, int ey, int ez, const Layout &L, float *dst0,
+                      float *dst1, cudaStream_t s);
+int launch_unpack_field(const float *src, int ex, int ey, int ez, const Layout &L, float *dst,
+                        cudaStream_t s);
+int launch_pack_coef(const float *src, const Layout &L, float *dst, cudaStream_t s);
+int launch_fill(float *dst, long long n, float v, cudaStream_t s);
+int launch_field_ref(int field, const float *in0, const float *in1, const float *in2,
+                     const ptk_fdtd_params &p, float *out, cudaStream_t s);
+int launch_h_half(const float *const in[6], float *const out[3], const ptk_fdtd_params &p,
+                  cudaStream_t s);
+int launch_e_half(const float *const e_in[3], const float *const h_new[3], float *const out[3],
+                  const ptk_fdtd_params &p, cudaStream_t s);
+
+// Extents of field f (0..5) in the reference layout.
+void field_extents(int f, int nx, int ny, int nz, int *ex, int *ey, int *ez);
+
+// Kernel launch counter (all launches issued by this library, graph nodes counted per replay).
+void count_launches(long long n);
+void count_graph_launch(long long nodes);
+void set_capturing(bool on);
+long long launches_issued();
+
+}  // namespace ptk
