@@ -2,14 +2,11 @@
 
 The compute path is libptask_gb300.so (hand-written CUDA kernels behind a C ABI, see
 include/ptask_gb300.h); the PTask-compatible C++ runtime is libptask_rt.so (include/ptask/).
-Importing this package loads the native library and raises ImportError if it has not been built:
-there is no CPU fallback.
+The native library is loaded on first use; every entry point raises ImportError if it has not been
+built: there is no CPU fallback.
 """
 from ._lib import LIB_PATH, PtkError, lib
-
-lib()
-
-from .fdtd import (FIELDS, Problem, Solver, device_info, field_extents, field_shape,  # noqa: E402
+from .fdtd import (FIELDS, Problem, Solver, device_info, field_extents, field_shape,
                    launch_count, random_fields, reference_params, solve, tuned_tiles, zero_fields)
 
 __all__ = ["LIB_PATH", "PtkError", "lib", "FIELDS", "Problem", "Solver", "device_info",
