@@ -294,13 +294,13 @@ def run_ours(args, wl, world, rank, local):
     d2h = sum(a.nbytes for a in zero)
 
     def e2e_step():
-        _lib.call("ptk_solver_set_fields", solver.handle, in_ptrs, P.PTK_HOST, None)
-        _lib.call("ptk_solver_set_coefficients", solver.handle, *[h.ptr.value for h in hcoef], P.PTK_HOST, None)
+        _lib.call("ptk_solver_set_fields", solver.handle, in_ptrs, _lib.PTK_HOST, None)
+        _lib.call("ptk_solver_set_coefficients", solver.handle, *[h.ptr.value for h in hcoef], _lib.PTK_HOST, None)
         _lib.call("ptk_solver_set_source", solver.handle, *prob.src, hwave.ptr.value, prob.wave.size,
-                  P.PTK_HOST, None)
+                  _lib.PTK_HOST, None)
         solver.reset_clock()
         solver.run(T)
-        _lib.call("ptk_solver_get_fields", solver.handle, out_ptrs, P.PTK_HOST, None)
+        _lib.call("ptk_solver_get_fields", solver.handle, out_ptrs, _lib.PTK_HOST, None)
 
     for _ in range(max(1, args.warmup)):
         e2e_step()

@@ -132,6 +132,26 @@ int ptk_launch_h_half_step(const float *const in[6], float *const out_h[3],
 int ptk_launch_e_half_step(const float *const e_in[3], const float *const h_new[3],
                            float *const out_e[3], const ptk_fdtd_params *p, void *stream);
 
+/* In-place half-step tasks of the cyclic FDTD graph with per-cell coefficients (dense reference
+ * layout; Da, Db, Ca, Cb have extents (Nx,Ny,Nz), wall nodes use the nearest cell).  They replace the
+ * three H tasks (graphfdtd.cpp:185-240) and the three E tasks (:243-312) of one step.
+ *   H' = Da*H + Db*curl(E)           E' = Ca*E + Cb*curl(H')  (PEC walls untouched)
+ * When wave/step_counter are given, wave[*step_counter] is added to Ez at interior node (si,sj,sk)
+ * after its update and *step_counter (a device int) is incremented. */
+int ptk_launch_h_step_coef(float *const h[3], const float *const e[3], const float *Da,
+                           const float *Db, const ptk_fdtd_params *p, void *stream);
+int ptk_launch_e_step_coef(float *const e[3], const float *const h[3], const float *Ca,
+                           const float *Cb, const ptk_fdtd_params *p, int si, int sj, int sk,
+                           const float *wave, int nwave, int *step_counter, void *stream);
+
+/* CUDA-graph capture of a sequence of launches on `stream` (the scheduler's replay of an iteration
+ * cycle; replaces per-task dispatch, ptask/task.cpp:3822-3900).  kernel_nodes is the number of
+ * kernels one replay runs (for the launch counter). */
+int ptk_capture_begin(void *stream);
+int ptk_capture_end(void *stream, void **graph_exec);
+int ptk_graph_exec_launch(void *graph_exec, void *stream, long long kernel_nodes);
+int ptk_graph_exec_destroy(void *graph_exec);
+
 /* ============================== device-resident solver ======================================== */
 /* One FDTD instance whose six fields, four coefficient arrays and source waveform stay in HBM.
  * The solver replays captured CUDA graphs of the fused Yee step (H then E in one kernel).  This is

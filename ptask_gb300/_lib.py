@@ -80,6 +80,13 @@ _SIGS = {
     "ptk_launch_h_half_step": (C.c_int, [C.POINTER(_P), C.POINTER(_P), C.POINTER(FdtdParams), _P]),
     "ptk_launch_e_half_step": (C.c_int, [C.POINTER(_P), C.POINTER(_P), C.POINTER(_P),
                                          C.POINTER(FdtdParams), _P]),
+    "ptk_launch_h_step_coef": (C.c_int, [C.POINTER(_P), C.POINTER(_P), _P, _P, C.POINTER(FdtdParams), _P]),
+    "ptk_launch_e_step_coef": (C.c_int, [C.POINTER(_P), C.POINTER(_P), _P, _P, C.POINTER(FdtdParams), C.c_int,
+                                         C.c_int, C.c_int, _P, C.c_int, _P, _P]),
+    "ptk_capture_begin": (C.c_int, [_P]),
+    "ptk_capture_end": (C.c_int, [_P, C.POINTER(_P)]),
+    "ptk_graph_exec_launch": (C.c_int, [_P, _P, C.c_longlong]),
+    "ptk_graph_exec_destroy": (C.c_int, [_P]),
     "ptk_solver_create": (C.c_int, [C.POINTER(FdtdParams), C.POINTER(_P)]),
     "ptk_solver_destroy": (C.c_int, [_P]),
     "ptk_solver_set_fields": (C.c_int, [_P, C.POINTER(_P), C.c_int, _P]),
