@@ -314,6 +314,8 @@ public:
     Datablock *m_iter_block = nullptr;
     UINT m_iter_max = 0, m_iter_count = 0;
     void *m_step_counter = nullptr;   // device int used by kernels that index a waveform by step
+    CyclePlan *m_loop_top = nullptr;     // this task heads a general-iteration loop
+    CyclePlan *m_loop_bottom = nullptr;  // this task owns the loop's MF_GENERAL_ITERATOR port
 
 private:
     Graph *m_graph;
@@ -328,6 +330,8 @@ struct GraphStats {
     UINT64 cycles_lowered = 0;     // iteration loops run as a captured / fused whole
     UINT64 cycle_iterations = 0;   // iterations executed inside lowered loops
     UINT64 graph_replays = 0;      // CUDA graph launches issued for lowered loops
+    float last_cycle_ms = 0;       // device time of the last lowered loop (CUDA events)
+    UINT last_cycle_iterations = 0;
 };
 
 class Graph : public Lockable {
@@ -389,6 +393,7 @@ private:
     std::string m_name;
     GRAPHSTATE m_state = PTGS_INITIALIZING;
     bool m_single = false;
+    bool m_scheduling = false;
     bool m_lower_cycles = true;
     bool m_fuse_cycles = true;
     std::thread m_thread;

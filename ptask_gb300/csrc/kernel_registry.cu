@@ -25,6 +25,11 @@ const KernelInfo kKernels[] = {
     {"EzComputation", 3, 1, (int)sizeof(ptk_fdtd_params)},   // :596
     {"HStep", 6, 3, (int)sizeof(ptk_fdtd_params)},           // the three H tasks in one launch
     {"EStep", 6, 3, (int)sizeof(ptk_fdtd_params)},           // the three E tasks in one launch
+    // Cyclic-graph half steps, in place, per-cell coefficients:
+    //   FDTDHStep(Hx,Hy,Hz,Ex,Ey,Ez, Da,Db, FDTD_PARAMS)
+    //   FDTDEStep(Ex,Ey,Ez,Hx,Hy,Hz, Ca,Cb, FDTD_PARAMS, SOURCE{i,j,k,n}, wave)
+    {"FDTDHStep", 8, 6, (int)sizeof(ptk_fdtd_params)},
+    {"FDTDEStep", 9, 6, (int)sizeof(ptk_fdtd_params) + 16},
 };
 const int kNumKernels = (int)(sizeof(kKernels) / sizeof(kKernels[0]));
 

@@ -1,0 +1,113 @@
+"""ctypes binding of the PTask FDTD graph C ABI (include/ptask_graph.h, libptask_rt.so)."""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from ._lib import FdtdParams, PtkError, lib
+from .fdtd import Problem, zero_fields
+
+RT_PATH = Path(__file__).resolve().parent / "_build" / "libptask_rt.so"
+
+CYCLIC_FUSED, CYCLIC_CAPTURED, CYCLIC_TASKWISE, UNROLLED = 0, 1, 2, 3
+MODES = {"fused": CYCLIC_FUSED, "captured": CYCLIC_CAPTURED, "taskwise": CYCLIC_TASKWISE, "unrolled": UNROLLED}
+
+
+class GraphStats(C.Structure):
+    _fields_ = [("dispatches", C.c_ulonglong), ("kernel_launches", C.c_ulonglong),
+                ("cycles_lowered", C.c_ulonglong), ("cycle_iterations", C.c_ulonglong),
+                ("graph_replays", C.c_ulonglong), ("last_cycle_ms", C.c_float), ("last_solve_ms", C.c_float)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+_rt = None
+_P = C.c_void_p
+_SIGS = {
+    "ptk_fdtd_graph_create": [C.POINTER(FdtdParams), C.c_int, C.c_int, C.POINTER(_P)],
+    "ptk_fdtd_graph_set_problem": [_P, _P, _P, _P, _P, C.c_int, C.c_int, C.c_int, _P, C.c_int],
+    "ptk_fdtd_graph_solve": [_P, C.POINTER(_P), C.c_int],
+    "ptk_fdtd_graph_solve_many": [_P, C.POINTER(_P), C.c_int, C.POINTER(_P), C.c_int],
+    "ptk_fdtd_graph_stats": [_P, C.POINTER(GraphStats)],
+    "ptk_fdtd_graph_write_dot": [_P, C.c_char_p],
+    "ptk_fdtd_graph_destroy": [_P],
+}
+
+
+def rt() -> C.CDLL:
+    global _rt
+    if _rt is None:
+        lib()   # the CUDA library first (libptask_rt.so links against it)
+        if not RT_PATH.exists():
+            raise ImportError(f"{RT_PATH} is missing: build with __graft_entry__.build()")
+        L = C.CDLL(str(RT_PATH))
+        for n, a in _SIGS.items():
+            getattr(L, n).argtypes = a
+            getattr(L, n).restype = C.c_int
+        _rt = L
+    return _rt
+
+
+def _check(rc: int, where: str) -> None:
+    if rc != 0:
+        raise PtkError(rc, where, lib().ptk_last_error().decode(errors="replace"))
+
+
+class FDTDGraph:
+    """The FDTD task graph on the PTask runtime (see ptask_graph.h for the forms)."""
+
+    def __init__(self, params: FdtdParams, mode: str = "fused", unrolled_steps: int = 0):
+        self.params = params
+        self.mode = mode
+        self._h = C.c_void_p()
+        _check(rt().ptk_fdtd_graph_create(C.byref(params), MODES[mode], unrolled_steps, C.byref(self._h)),
+               "ptk_fdtd_graph_create")
+
+    def set_problem(self, prob: Problem | None) -> None:
+        if prob is None:
+            _check(rt().ptk_fdtd_graph_set_problem(self._h, None, None, None, None, -1, -1, -1, None, 0),
+                   "set_problem")
+            return
+        self._coefs = [np.ascontiguousarray(a, np.float32) for a in (prob.Ca, prob.Cb, prob.Da, prob.Db)]
+        self._wave = np.ascontiguousarray(prob.wave, np.float32)
+        si, sj, sk = prob.src if prob.has_source else (-1, -1, -1)
+        _check(rt().ptk_fdtd_graph_set_problem(self._h, *[a.ctypes.data for a in self._coefs], si, sj, sk,
+                                               self._wave.ctypes.data if self._wave.size else None,
+                                               int(self._wave.size)), "set_problem")
+
+    def solve(self, fields, steps: int) -> list[np.ndarray]:
+        out = [np.array(f, np.float32, copy=True, order="C") for f in fields]
+        ptrs = (C.c_void_p * 6)(*[a.ctypes.data for a in out])
+        _check(rt().ptk_fdtd_graph_solve(self._h, ptrs, steps), "ptk_fdtd_graph_solve")
+        return out
+
+    def solve_many(self, fields, instances: int, steps: int) -> list[list[np.ndarray]]:
+        ins = [np.ascontiguousarray(f, np.float32) for f in fields]
+        nx, ny, nz = self.params.Nx, self.params.Ny, self.params.Nz
+        res = [zero_fields(nx, ny, nz) for _ in range(instances)]
+        rptrs = (C.c_void_p * (6 * instances))(*[a.ctypes.data for r in res for a in r])
+        _check(rt().ptk_fdtd_graph_solve_many(self._h, (C.c_void_p * 6)(*[a.ctypes.data for a in ins]),
+                                              instances, rptrs, steps), "solve_many")
+        return res
+
+    def stats(self) -> dict:
+        s = GraphStats()
+        _check(rt().ptk_fdtd_graph_stats(self._h, C.byref(s)), "stats")
+        return s.as_dict()
+
+    def write_dot(self, path: str) -> None:
+        _check(rt().ptk_fdtd_graph_write_dot(self._h, str(path).encode()), "write_dot")
+
+    def close(self) -> None:
+        if self._h:
+            rt().ptk_fdtd_graph_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -45,6 +45,31 @@ void vlog(FILE *f, const char *prefix, const char *fmt, va_list ap)
 
 void *runtime_io_stream() { return g_io_stream; }
 
+// Streams handed to graphs; kept for the life of the process because blocks may be freed on them
+// after their graph is gone.
+static std::mutex g_stream_mu;
+static std::vector<void *> g_free_streams;
+
+void *acquire_stream()
+{
+    std::lock_guard<std::mutex> lk(g_stream_mu);
+    if (!g_free_streams.empty()) {
+        void *s = g_free_streams.back();
+        g_free_streams.pop_back();
+        return s;
+    }
+    void *s = nullptr;
+    return ptk_stream_create(&s) == PTK_OK ? s : nullptr;
+}
+
+void release_stream(void *s)
+{
+    if (!s) return;
+    ptk_stream_sync(s);
+    std::lock_guard<std::mutex> lk(g_stream_mu);
+    g_free_streams.push_back(s);
+}
+
 const char *ControlSignalString(CONTROLSIGNAL s)
 {
     static const char *names[] = {"DBCTLC_NONE", "DBCTLC_BOF", "DBCTLC_EOF", "DBCTLC_BEGINITERATION",
@@ -247,7 +272,9 @@ PTRESULT Terminate()
     ptk_stream_sync(g_io_stream);
     ptk_stream_destroy(g_io_stream);
     g_io_stream = nullptr;
-    for (auto &kv : g_templates) delete kv.second;
+    std::set<DatablockTemplate *> uniq;
+    for (auto &kv : g_templates) uniq.insert(kv.second);
+    for (DatablockTemplate *t : uniq) delete t;
     g_templates.clear();
     for (auto &kv : g_kernels) delete kv.second;
     g_kernels.clear();
@@ -261,12 +288,16 @@ BOOL IsInitialized() { return g_init; }
 DatablockTemplate *GetDatablockTemplate(const char *name, unsigned int stride, unsigned int x, unsigned int y,
                                         unsigned int z, bool rec, bool raw)
 {
+    // A template is identified by its name and shape: graphs of different sizes that reuse a name
+    // (every FDTD graph calls its field templates "HxSize" ...) get distinct templates.
     std::lock_guard<std::mutex> lk(g_mu);
-    std::string key = name ? name : "";
+    std::string key = std::string(name ? name : "") + "#" + std::to_string(stride) + "," + std::to_string(x) +
+                      "," + std::to_string(y) + "," + std::to_string(z) + (rec ? "r" : "") + (raw ? "b" : "");
     auto it = g_templates.find(key);
     if (it != g_templates.end()) return it->second;
     auto *t = new DatablockTemplate(name, stride, x, y, z, rec, raw);
     g_templates[key] = t;
+    g_templates[name ? name : ""] = t;   // latest template of this name, for lookup by name
     return t;
 }
 
