@@ -11,24 +11,38 @@ from ptask_gb300 import _lib
 from conftest import ROOT
 
 
-def declared_symbols():
+# header -> shared library that must export its entry points
+HEADERS = {"ptask_gb300.h": "libptask_gb300.so", "ptask_graph.h": "libptask_rt.so"}
+
+
+def declared_symbols(header=None):
     names = set()
     for h in (ROOT / "include").glob("*.h"):
+        if header and h.name != header:
+            continue
         text = h.read_text()
         names |= set(re.findall(r"\b(ptk_[a-z0-9_]+)\s*\(", text))
     return sorted(names)
 
 
-def test_library_exports_every_declared_symbol():
-    lib = C.CDLL(str(_lib.LIB_PATH))
-    missing = [n for n in declared_symbols() if not hasattr(lib, n)]
+def test_every_header_is_mapped_to_a_library():
+    assert {h.name for h in (ROOT / "include").glob("*.h")} == set(HEADERS)
+
+
+@pytest.mark.parametrize("header,libname", sorted(HEADERS.items()))
+def test_library_exports_every_declared_symbol(header, libname):
+    C.CDLL(str(_lib.LIB_PATH), mode=C.RTLD_GLOBAL)
+    lib = C.CDLL(str(_lib.LIB_PATH.parent / libname))
+    names = declared_symbols(header)
+    missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
-    assert len(declared_symbols()) >= 40
+    assert len(names) >= 7
 
 
-def test_python_binding_covers_header():
-    bound = set(_lib.exported_symbols())
-    assert set(declared_symbols()) <= bound | {"ptk_nothing"}, sorted(set(declared_symbols()) - bound)
+def test_python_binding_covers_headers():
+    from ptask_gb300 import graph
+    bound = set(_lib.exported_symbols()) | set(graph._SIGS)
+    assert set(declared_symbols()) <= bound, sorted(set(declared_symbols()) - bound)
 
 
 def test_kernel_registry_resolves_reference_entries():
