@@ -236,8 +236,10 @@ def run_ours(args, wl, world, rank, local):
                               source_mode=1, seed=2 + rank)
     cells = nx * ny * nz
     tiles = None
-    if not args.no_autotune:
-        tiles = P.tuned_tiles(nx, ny, nz) if hasattr(P, "tuned_tiles") else None
+    if args.tiles:
+        tiles = tuple(int(v) for v in args.tiles.split(","))
+    elif not args.no_autotune:
+        tiles = P.tuned_tiles(nx, ny, nz)
 
     solver = P.Solver(prob.params)
     if tiles:
@@ -348,18 +350,85 @@ def run_ours(args, wl, world, rank, local):
     return 0
 
 
+def run_served(args, kind, world, rank, local):
+    """Batched (all requests at t=0) or served (Poisson arrivals) FDTD: continuous batching against
+    plain one-at-a-time dispatch of the same requests."""
+    import ptask_gb300 as P
+    from ptask_gb300 import _lib
+    from ptask_gb300.serve import Server, batched_instances, poisson_trace
+
+    _lib.call("ptk_runtime_init", local)
+    if kind == "batched":
+        reqs = batched_instances(64, seed=4 + rank)
+        scale = 0.0
+        desc = ("batched FDTD: 64 instances in one persistent fused launch per step, edges per axis uniform "
+                "in [32,192], steps uniform in [100,2000], 1-8 dielectric boxes, seeded sources, FP32")
+    else:
+        n = args.requests
+        reqs = poisson_trace(n, rate=200.0, seed=5 + rank)
+        scale = 1.0
+        desc = (f"served FDTD: Poisson arrivals 200 req/s, {n} requests (the workload's 20k-request trace "
+                "shortened), cube edge log-uniform in [24,256], steps uniform in [50,1000], FP32, "
+                "admission by HBM budget")
+    cells = sum(r.cell_updates for r in reqs)
+
+    def serve(max_active):
+        with Server(max_active=max_active, chunk_steps=32, persistent=True) as s:
+            for r in reqs:
+                s.submit(r)
+            l0 = P.launch_count()
+            s.run(time_scale=scale)
+            st = s.stats()
+            st["launches"] = P.launch_count() - l0
+            return st
+
+    for _ in range(args.warmup if kind == "batched" else 0):
+        serve(0)
+    clocks = ClockSampler(local)
+    clocks.start()
+    runs = [serve(0) for _ in range(args.steps)]
+    clk = clocks.stop()
+    plain = serve(1)
+    best = min(runs, key=lambda s: s["wall_s"])
+    wall = statistics.median(s["wall_s"] for s in runs)
+    value = len(reqs) / wall
+    line = {
+        "metric": f"FDTD {kind} solves/s", "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded request generator)",
+        "config": {"workload": desc, "requests": len(reqs), "cell_updates": cells,
+                   "bench_step": "serve the whole request set", "l2": "working set larger than L2"},
+        "mcell_updates_per_s": cells / wall / 1e6,
+        "p50_latency_s": best["p50_latency_s"], "p99_latency_s": best["p99_latency_s"],
+        "peak_active": best["peak_active"], "peak_bytes": best["peak_bytes"],
+        "plain": {"solves_per_s": len(reqs) / plain["wall_s"], "mcell_updates_per_s": cells / plain["wall_s"] / 1e6,
+                  "p50_latency_s": plain["p50_latency_s"], "p99_latency_s": plain["p99_latency_s"],
+                  "wall_s": plain["wall_s"]},
+        "speedup_vs_plain": (len(reqs) / wall) / (len(reqs) / plain["wall_s"]),
+        "gpu_launches": int(best["launches"]),
+        "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="plain256")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batched", "served"], default="plain256")
+    ap.add_argument("--requests", type=int, default=1000, help="served workload: requests in the trace")
+    ap.add_argument("--tiles", default=None, help="fixed tile shape ROWS,DEPTH (skips the autotuner)")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     world, rank, local = dist_env()
-    wl = WORKLOADS[args.workload]
+    if args.workload in ("batched", "served") and args.impl == "ours":
+        return run_served(args, args.workload, world, rank, local)
+    wl = WORKLOADS.get(args.workload, WORKLOADS["plain256"])
     if args.impl == "reference":
         return run_reference(args, wl, world, rank, local)
     return run_ours(args, wl, world, rank, local)

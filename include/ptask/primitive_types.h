@@ -5,9 +5,11 @@
 #ifndef PTASK_GB300_PRIMITIVE_TYPES_H
 #define PTASK_GB300_PRIMITIVE_TYPES_H
 
+#include <cmath>   // the reference's Win32 headers make fabs/sqrt visible to its sources
 #include <cstddef>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #ifndef _WIN32

@@ -202,6 +202,57 @@ int ptk_fdtd_solve(const ptk_fdtd_params *p, float *const fields[6], const float
                    const float *Cb, const float *Da, const float *Db, int si, int sj, int sk,
                    const float *wave, int nwave, int steps, float *ms);
 
+/* ============================== batched / served FDTD ========================================= */
+/* Many device-resident FDTD instances of uneven size advanced together: every time step of every
+ * active instance is one persistent launch of the fused step kernel over the concatenated tile lists,
+ * chunks of steps are replayed as CUDA graphs, and requests are admitted continuously by HBM budget
+ * as earlier ones finish.  No reference counterpart: the reference pipelines numBlocks copies of one
+ * problem through one graph (graphfdtd.cpp:1076-1097) with one dispatch per task per copy. */
+
+typedef struct ptk_server ptk_server;
+struct ptk_problem_desc;   /* defined with the problem generator below */
+
+typedef struct ptk_server_config {
+    size_t hbm_budget_bytes;   /* device bytes the admitted instances may hold (0: 80% of free HBM) */
+    int max_active;            /* instance slots (0: unlimited; 1: plain one-at-a-time dispatch) */
+    int chunk_steps;           /* steps per replayed graph between admission points (0: 32) */
+    int tile_rows;             /* fused-kernel tile rows 4, 8 or 16 (0: 8) */
+    int keep_results;          /* keep finished fields for ptk_server_fetch */
+    int persistent;            /* persistent grid of resident CTAs instead of one CTA per tile */
+} ptk_server_config;
+
+typedef struct ptk_request_info {
+    long long ticket;
+    int Nx, Ny, Nz, steps;
+    double arrival_s, admit_s, finish_s;   /* run clock; admit/finish < 0 when not yet */
+    double checksum[6];                    /* FP64 sums of the six result fields */
+    int done;
+} ptk_request_info;
+
+typedef struct ptk_server_stats {
+    long long submitted, completed;
+    double wall_s;                 /* time spent in ptk_server_run */
+    double solves_per_s;
+    double p50_latency_s, p99_latency_s, mean_latency_s;   /* finish - arrival */
+    double cell_updates, mcells_per_s;
+    long long chunks, kernel_launches;
+    int peak_active;
+    size_t peak_bytes;
+} ptk_server_stats;
+
+int ptk_server_create(const ptk_server_config *cfg, ptk_server **out);
+/* Queue a request: a seeded problem (ptk_problem_desc) with zero initial fields, arriving at
+ * arrival_s on the trace clock.  Rejects requests larger than the whole budget. */
+int ptk_server_submit(ptk_server *s, const struct ptk_problem_desc *d, double arrival_s, long long *ticket);
+/* Serve every queued request.  Arrival times are multiplied by time_scale (0: all available at
+ * once); requests are admitted in arrival order as they arrive and fit. */
+int ptk_server_run(ptk_server *s, double time_scale);
+int ptk_server_request(ptk_server *s, long long ticket, ptk_request_info *info);
+/* Host copy of a finished request's fields (reference layout); needs keep_results. */
+int ptk_server_fetch(ptk_server *s, long long ticket, float *const fields[6]);
+int ptk_server_stats_get(ptk_server *s, ptk_server_stats *st);
+int ptk_server_destroy(ptk_server *s);
+
 /* ============================== autotuner ===================================================== */
 /* Time candidate tile shapes for a grid of the given size on the current device and return the
  * fastest (cached per shape for the life of the process). */

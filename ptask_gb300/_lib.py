@@ -37,6 +37,28 @@ class ProblemDesc(C.Structure):
                 ("source_mode", C.c_int), ("seed", C.c_uint64)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_active", C.c_int), ("chunk_steps", C.c_int),
+                ("tile_rows", C.c_int), ("keep_results", C.c_int), ("persistent", C.c_int)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("ticket", C.c_longlong), ("Nx", C.c_int), ("Ny", C.c_int), ("Nz", C.c_int), ("steps", C.c_int),
+                ("arrival_s", C.c_double), ("admit_s", C.c_double), ("finish_s", C.c_double),
+                ("checksum", C.c_double * 6), ("done", C.c_int)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("completed", C.c_longlong), ("wall_s", C.c_double),
+                ("solves_per_s", C.c_double), ("p50_latency_s", C.c_double), ("p99_latency_s", C.c_double),
+                ("mean_latency_s", C.c_double), ("cell_updates", C.c_double), ("mcells_per_s", C.c_double),
+                ("chunks", C.c_longlong), ("kernel_launches", C.c_longlong), ("peak_active", C.c_int),
+                ("peak_bytes", C.c_size_t)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 class PtkError(RuntimeError):
     def __init__(self, code: int, where: str, msg: str):
         super().__init__(f"{where}: PTK_ERR_{ERRORS.get(code, code)}: {msg}")
@@ -102,7 +124,14 @@ _SIGS = {
     "ptk_solver_last_launches": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "ptk_fdtd_solve": (C.c_int, [C.POINTER(FdtdParams), C.POINTER(_P), _P, _P, _P, _P, C.c_int, C.c_int,
                                  C.c_int, _P, C.c_int, C.c_int, C.POINTER(C.c_float)]),
-    "ptk_autotune_tiles": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(TileConfig), C.POINTER(C.c_float)]),
+    "ptk_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(_P)]),
+    "ptk_server_submit": (C.c_int, [_P, C.POINTER(ProblemDesc), C.c_double, C.POINTER(C.c_longlong)]),
+    "ptk_server_run": (C.c_int, [_P, C.c_double]),
+    "ptk_server_request": (C.c_int, [_P, C.c_longlong, C.POINTER(RequestInfo)]),
+    "ptk_server_fetch": (C.c_int, [_P, C.c_longlong, C.POINTER(_P)]),
+    "ptk_server_stats_get": (C.c_int, [_P, C.POINTER(ServerStats)]),
+    "ptk_server_destroy": (C.c_int, [_P]),
+    "ptk_autotune_tiles":(C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(TileConfig), C.POINTER(C.c_float)]),
     "ptk_problem_generate": (C.c_int, [C.POINTER(ProblemDesc), C.POINTER(FdtdParams), _P, _P, _P, _P,
                                        C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), _P]),
     "ptk_reference_params": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(FdtdParams)]),

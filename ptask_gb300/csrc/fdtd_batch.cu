@@ -1,0 +1,517 @@
+// fdtd_batch.cu -- batched and served FDTD: many device-resident instances of uneven size advanced
+// together by the fused step kernel, with continuous admission by HBM budget.
+//
+// One time step of every active instance is ONE launch of k_yee_step over the concatenated tile
+// lists of all instances (a persistent grid of resident CTAs walks the list), and chunks of steps
+// are replayed as captured CUDA graphs.  Instances finish at their own step counts: their tiles go
+// idle inside the chunk in which they finish and they leave the batch at the chunk boundary, where
+// newly arrived requests are admitted if their fields fit the HBM budget.  Request problems are
+// generated on the device (coefficients from the seeded box list), so admission moves only the
+// source waveform over the host link.
+//
+// The reference has no batching: it pipelines numBlocks copies of one problem through one graph
+// (graphfdtd.cpp:1076-1097) and dispatches every task of every copy separately.
+#include "ptk_internal.h"
+#include "ptk_problem.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <map>
+#include <mutex>
+#include <thread>
+#include <tuple>
+#include <vector>
+
+namespace ptk {
+
+constexpr int kMaxBoxes = 64;
+
+struct BoxArgs {
+    int n;
+    int lo[kMaxBoxes][3];
+    int hi[kMaxBoxes][3];
+    float epsr[kMaxBoxes];
+};
+
+// Padded coefficients of a generated problem: the device twin of ptk_problem_generate (same boxes,
+// same FP32 expressions Cb = Dt/(eps0*eps_r), Db = Dt/mu0; wall nodes take the nearest cell).
+__global__ void k_generate_coefs(BoxArgs boxes, int nx, int ny, int nz, int pitch, long long plane, float dt,
+                                 float eps0, float mu0, float *Ca, float *Cb, float *Da, float *Db)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y, k = blockIdx.z;
+    if (i > nx) return;
+    const int ci = min(i, nx - 1), cj = min(j, ny - 1), ck = min(k, nz - 1);
+    float e = 1.0f;
+    for (int b = boxes.n - 1; b >= 0; --b)
+        if (ci >= boxes.lo[b][0] && ci < boxes.hi[b][0] && cj >= boxes.lo[b][1] && cj < boxes.hi[b][1] &&
+            ck >= boxes.lo[b][2] && ck < boxes.hi[b][2]) {
+            e = boxes.epsr[b];
+            break;
+        }
+    const long long o = i + (long long)pitch * j + plane * k;
+    Ca[o] = 1.0f;
+    Cb[o] = __fdiv_rn(dt, __fmul_rn(eps0, e));
+    Da[o] = 1.0f;
+    Db[o] = __fdiv_rn(dt, mu0);
+}
+
+// Sum of each valid field element (FP64; order of accumulation not fixed, for reporting only).
+__global__ void k_checksum(const float *__restrict__ f, int ex, int ey, int ez, int pitch, long long plane,
+                           double *out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y, k = blockIdx.z;
+    double v = (i < ex) ? (double)f[i + (long long)pitch * j + plane * k] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(out, v);
+}
+
+struct Inst {
+    long long ticket = -1;
+    ptk_problem_desc desc{};
+    ptk_fdtd_params p{};
+    Layout L{};
+    float *buf[2][6] = {};
+    float *coef[4] = {};
+    float *wave = nullptr;
+    int nwave = 0;
+    long long src = -1;
+    int steps_total = 0, done = 0;
+    size_t bytes = 0;
+    double t_arrival = 0, t_admit = -1, t_finish = -1;
+    double t_arrival_run = 0;   // arrival on the run's clock (scaled trace time)
+    double *d_sum = nullptr;
+    double checksum[6] = {};
+    std::vector<float> result[6];
+    bool finished = false;
+};
+
+size_t instance_bytes(const Layout &L, int nwave)
+{
+    return (size_t)L.total * sizeof(float) * 16 + (size_t)nwave * sizeof(float) + 6 * sizeof(double) + 4096;
+}
+
+}  // namespace ptk
+
+using namespace ptk;
+
+struct ptk_server {
+    ptk_server_config cfg{};
+    cudaStream_t st = nullptr;
+    std::vector<Inst *> all;        // every submitted request, by ticket
+    std::vector<Inst *> active;     // admitted, running
+    size_t next = 0;                // next request to admit (arrival order)
+    size_t used = 0, peak_bytes = 0;
+    int peak_active = 0;
+    // device work list
+    InstDesc *d_desc = nullptr;
+    int *d_tile0 = nullptr;
+    InstDesc *h_desc = nullptr;     // pinned staging
+    int *h_tile0 = nullptr;
+    int cap = 0;
+    int total_tiles = 0;
+    bool dirty = true;
+    std::map<std::tuple<int, int, int, int>, cudaGraphExec_t> graphs;
+    long long chunks = 0, launches = 0;
+    double wall_s = 0, cell_updates = 0;
+    double t0_wall = 0;
+    std::mutex mu;
+};
+
+namespace {
+
+double now_s()
+{
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+int grow_worklist(ptk_server *s, int n)
+{
+    if (n <= s->cap) return PTK_OK;
+    int cap = std::max(n, 2 * s->cap);
+    if (s->d_desc) {
+        cudaStreamSynchronize(s->st);
+        pool_free(s->d_desc, s->st);
+        pool_free(s->d_tile0, s->st);
+        cudaFreeHost(s->h_desc);
+        cudaFreeHost(s->h_tile0);
+    }
+    int rc = pool_alloc(sizeof(InstDesc) * cap, s->st, (void **)&s->d_desc);
+    if (!rc) rc = pool_alloc(sizeof(int) * (cap + 1), s->st, (void **)&s->d_tile0);
+    if (rc) return rc;
+    PTK_CUDA_TRY(cudaMallocHost(&s->h_desc, sizeof(InstDesc) * cap));
+    PTK_CUDA_TRY(cudaMallocHost(&s->h_tile0, sizeof(int) * (cap + 1)));
+    s->cap = cap;
+    for (auto &kv : s->graphs) cudaGraphExecDestroy(kv.second);
+    s->graphs.clear();
+    return PTK_OK;
+}
+
+int admit(ptk_server *s, Inst *in)
+{
+    std::vector<BoxSpec> boxes;
+    std::vector<float> wave;
+    int si, sj, sk;
+    int rc = problem_plan(&in->desc, &in->p, &boxes, &si, &sj, &sk, &wave);
+    if (rc) return set_error(rc, "bad request descriptor");
+    if ((int)boxes.size() > kMaxBoxes) return set_error(PTK_ERR_INVALID, "at most %d boxes per request", kMaxBoxes);
+    in->L = make_layout(in->p.Nx, in->p.Ny, in->p.Nz);
+    in->steps_total = in->desc.steps;
+    const size_t bytes = (size_t)in->L.total * sizeof(float);
+    cudaStream_t st = s->st;
+    for (int b = 0; b < 2 && !rc; ++b)
+        for (int f = 0; f < 6 && !rc; ++f) rc = pool_alloc(bytes, st, (void **)&in->buf[b][f]);
+    for (int c = 0; c < 4 && !rc; ++c) rc = pool_alloc(bytes, st, (void **)&in->coef[c]);
+    if (!rc) rc = pool_alloc(6 * sizeof(double), st, (void **)&in->d_sum);
+    in->nwave = (si >= 0 && !wave.empty()) ? (int)wave.size() : 0;
+    if (!rc && in->nwave) rc = pool_alloc(wave.size() * sizeof(float), st, (void **)&in->wave);
+    if (rc) return rc;
+    for (int b = 0; b < 2; ++b)
+        for (int f = 0; f < 6; ++f) PTK_CUDA_TRY(cudaMemsetAsync(in->buf[b][f], 0, bytes, st));
+    BoxArgs ba{};
+    ba.n = (int)boxes.size();
+    for (int b = 0; b < ba.n; ++b) {
+        for (int a = 0; a < 3; ++a) {
+            ba.lo[b][a] = boxes[b].lo[a];
+            ba.hi[b][a] = boxes[b].hi[a];
+        }
+        ba.epsr[b] = boxes[b].epsr;
+    }
+    dim3 grid((in->L.nx + 1 + 127) / 128, in->L.ny + 1, in->L.nz + 1);
+    k_generate_coefs<<<grid, 128, 0, st>>>(ba, in->L.nx, in->L.ny, in->L.nz, in->L.pitch, in->L.plane, in->p.Dt,
+                                           in->p.eps0, in->p.mu0, in->coef[0], in->coef[1], in->coef[2], in->coef[3]);
+    PTK_CUDA_TRY(cudaGetLastError());
+    count_launches(1);
+    if (in->nwave) {
+        // pageable source: the copy is staged before this returns, so `wave` may go out of scope
+        PTK_CUDA_TRY(cudaMemcpyAsync(in->wave, wave.data(), wave.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+        in->src = (long long)si + (long long)in->L.pitch * sj + in->L.plane * sk;
+    }
+    in->bytes = instance_bytes(in->L, in->nwave);
+    s->used += in->bytes;
+    s->peak_bytes = std::max(s->peak_bytes, s->used);
+    s->active.push_back(in);
+    s->peak_active = std::max(s->peak_active, (int)s->active.size());
+    s->dirty = true;
+    return PTK_OK;
+}
+
+void release(ptk_server *s, Inst *in)
+{
+    for (int b = 0; b < 2; ++b)
+        for (int f = 0; f < 6; ++f) pool_free(in->buf[b][f], s->st);
+    for (int c = 0; c < 4; ++c) pool_free(in->coef[c], s->st);
+    pool_free(in->wave, s->st);
+    pool_free(in->d_sum, s->st);
+    for (int b = 0; b < 2; ++b)
+        for (int f = 0; f < 6; ++f) in->buf[b][f] = nullptr;
+    s->used -= in->bytes;
+}
+
+int rebuild_worklist(ptk_server *s)
+{
+    const int n = (int)s->active.size();
+    int rc = grow_worklist(s, n);
+    if (rc) return rc;
+    cudaStreamSynchronize(s->st);   // the pinned staging may still feed a previous copy
+    int tiles = 0;
+    for (int q = 0; q < n; ++q) {
+        Inst *in = s->active[q];
+        InstDesc d{};
+        for (int b = 0; b < 2; ++b)
+            for (int f = 0; f < 6; ++f) d.buf[b][f] = in->buf[b][f];
+        for (int c = 0; c < 4; ++c) d.coef[c] = in->coef[c];
+        d.wave = in->wave;
+        d.plane = in->L.plane;
+        d.nx = in->L.nx; d.ny = in->L.ny; d.nz = in->L.nz; d.pitch = in->L.pitch;
+        d.cx = in->p.Cx; d.cy = in->p.Cy; d.cz = in->p.Cz;
+        d.src = in->nwave ? in->src : -1;
+        d.nwave = in->nwave;
+        d.step = in->done;
+        d.steps_left = in->steps_total - in->done;
+        plan_tiles(d, s->cfg.tile_rows, in->L.nz > 48 ? 16 : 0);
+        s->h_desc[q] = d;
+        s->h_tile0[q] = tiles;
+        tiles += d.tiles_x * d.tiles_y * d.tiles_z + d.face_tiles;
+    }
+    s->h_tile0[n] = tiles;
+    s->total_tiles = tiles;
+    if (n) {
+        PTK_CUDA_TRY(cudaMemcpyAsync(s->d_desc, s->h_desc, sizeof(InstDesc) * n, cudaMemcpyHostToDevice, s->st));
+        PTK_CUDA_TRY(cudaMemcpyAsync(s->d_tile0, s->h_tile0, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s->st));
+    }
+    s->dirty = false;
+    return PTK_OK;
+}
+
+int chunk_graph(ptk_server *s, int len, int grid, cudaGraphExec_t *out)
+{
+    const int n = (int)s->active.size();
+    auto key = std::make_tuple(len, n, s->total_tiles, grid);
+    auto it = s->graphs.find(key);
+    if (it != s->graphs.end()) {
+        *out = it->second;
+        return PTK_OK;
+    }
+    cudaStream_t cap;
+    PTK_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    PTK_CUDA_TRY(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+    set_capturing(true);
+    int rc = PTK_OK;
+    for (int q = 0; q < len && !rc; ++q)
+        rc = launch_yee_step_grid(s->d_desc, s->d_tile0, n, s->total_tiles, q, s->cfg.tile_rows, grid, cap);
+    if (!rc) rc = launch_advance(s->d_desc, n, len, cap);
+    set_capturing(false);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(cap, &g);
+    cudaStreamDestroy(cap);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return set_error(PTK_ERR_CUDA, "chunk capture: %s", cudaGetErrorString(e));
+    cudaGraphExec_t ex;
+    e = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return set_error(PTK_ERR_CUDA, "chunk instantiate: %s", cudaGetErrorString(e));
+    s->graphs[key] = ex;
+    *out = ex;
+    return PTK_OK;
+}
+
+int retire(ptk_server *s, Inst *in, double t)
+{
+    const int par = in->done & 1;
+    PTK_CUDA_TRY(cudaMemsetAsync(in->d_sum, 0, 6 * sizeof(double), s->st));
+    for (int f = 0; f < 6; ++f) {
+        int ex, ey, ez;
+        field_extents(f, in->L.nx, in->L.ny, in->L.nz, &ex, &ey, &ez);
+        dim3 grid((ex + 127) / 128, ey, ez);
+        k_checksum<<<grid, 128, 0, s->st>>>(in->buf[par][f], ex, ey, ez, in->L.pitch, in->L.plane, in->d_sum + f);
+        count_launches(1);
+        if (s->cfg.keep_results) {
+            in->result[f].resize((size_t)ex * ey * ez);
+            float *stage = nullptr;
+            int rc = pool_alloc(in->result[f].size() * sizeof(float), s->st, (void **)&stage);
+            if (rc) return rc;
+            rc = launch_unpack_field(in->buf[par][f], ex, ey, ez, in->L, stage, s->st);
+            if (rc) return rc;
+            PTK_CUDA_TRY(cudaMemcpyAsync(in->result[f].data(), stage, in->result[f].size() * sizeof(float),
+                                         cudaMemcpyDeviceToHost, s->st));
+            pool_free(stage, s->st);
+        }
+    }
+    PTK_CUDA_TRY(cudaMemcpyAsync(in->checksum, in->d_sum, 6 * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+    PTK_CUDA_TRY(cudaStreamSynchronize(s->st));
+    in->t_finish = t;
+    in->finished = true;
+    s->cell_updates += (double)in->L.nx * in->L.ny * in->L.nz * in->steps_total;
+    release(s, in);
+    return PTK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ptk_server_create(const ptk_server_config *cfg, ptk_server **out)
+{
+    clear_error();
+    PTK_CHECK_ARG(cfg && out, "NULL argument");
+    int rc = ensure_init();
+    if (rc) return rc;
+    auto *s = new ptk_server();
+    s->cfg = *cfg;
+    if (s->cfg.max_active <= 0) s->cfg.max_active = 1 << 20;
+    if (s->cfg.chunk_steps <= 0) s->cfg.chunk_steps = 32;
+    if (s->cfg.tile_rows != 4 && s->cfg.tile_rows != 8 && s->cfg.tile_rows != 16) s->cfg.tile_rows = 8;
+    if (s->cfg.hbm_budget_bytes == 0) {
+        size_t f = 0, t = 0;
+        cudaMemGetInfo(&f, &t);
+        s->cfg.hbm_budget_bytes = f / 10 * 8;
+    }
+    if (cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) != cudaSuccess) {
+        delete s;
+        return set_error(PTK_ERR_CUDA, "stream creation failed");
+    }
+    *out = s;
+    return PTK_OK;
+}
+
+int ptk_server_submit(ptk_server *s, const ptk_problem_desc *d, double arrival_s, long long *ticket)
+{
+    PTK_CHECK_ARG(s && d, "NULL argument");
+    PTK_CHECK_ARG(d->Nx >= 1 && d->Ny >= 1 && d->Nz >= 1 && d->steps >= 1, "bad request %dx%dx%d x %d steps",
+                  d->Nx, d->Ny, d->Nz, d->steps);
+    PTK_CHECK_ARG(d->n_boxes <= kMaxBoxes, "at most %d boxes per request", kMaxBoxes);
+    const Layout L = make_layout(d->Nx, d->Ny, d->Nz);
+    const size_t need = instance_bytes(L, d->steps);
+    if (need > s->cfg.hbm_budget_bytes)
+        return set_error(PTK_ERR_BUDGET, "request needs %zu bytes, more than the whole HBM budget (%zu)", need,
+                         s->cfg.hbm_budget_bytes);
+    std::lock_guard<std::mutex> lk(s->mu);
+    Inst *in = new Inst();
+    in->ticket = (long long)s->all.size();
+    in->desc = *d;
+    in->t_arrival = arrival_s;
+    s->all.push_back(in);
+    if (ticket) *ticket = in->ticket;
+    return PTK_OK;
+}
+
+int ptk_server_run(ptk_server *s, double time_scale)
+{
+    clear_error();
+    PTK_CHECK_ARG(s, "NULL server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    // admission order = arrival order (stable for ties)
+    std::vector<Inst *> order;
+    for (Inst *in : s->all)
+        if (!in->finished && in->t_admit < 0) order.push_back(in);
+    std::stable_sort(order.begin(), order.end(), [](Inst *a, Inst *b) { return a->t_arrival < b->t_arrival; });
+    for (Inst *in : order) in->t_arrival_run = time_scale > 0 ? in->t_arrival * time_scale : 0.0;
+    const double t0 = now_s();
+    size_t nxt = 0;
+    const int grid_cap = std::max(1, yee_resident_ctas(s->cfg.tile_rows));
+    auto clock = [&] { return (now_s() - t0); };
+    auto arrived = [&](Inst *in, double t) { return time_scale <= 0 || in->t_arrival * time_scale <= t; };
+    int rc = PTK_OK;
+    while ((nxt < order.size() || !s->active.empty()) && rc == PTK_OK) {
+        double t = clock();
+        // admit arrived requests, FIFO, while they fit the budget and the slot limit
+        while (nxt < order.size() && arrived(order[nxt], t) && (int)s->active.size() < s->cfg.max_active) {
+            Inst *in = order[nxt];
+            const size_t need = instance_bytes(make_layout(in->desc.Nx, in->desc.Ny, in->desc.Nz), in->desc.steps);
+            if (s->used + need > s->cfg.hbm_budget_bytes) break;
+            in->t_admit = t;
+            rc = admit(s, in);
+            if (rc) break;
+            ++nxt;
+        }
+        if (rc) break;
+        if (s->active.empty()) {
+            if (nxt < order.size()) {
+                const double wait = order[nxt]->t_arrival * time_scale - clock();
+                if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.01)));
+            }
+            continue;
+        }
+        if (s->dirty) rc = rebuild_worklist(s);
+        if (rc) break;
+        int left_min = 1 << 30;
+        for (Inst *in : s->active) left_min = std::min(left_min, in->steps_total - in->done);
+        // chunk length: the configured chunk, shortened so that the first finisher leaves promptly
+        const int len = std::max(1, std::min(s->cfg.chunk_steps, left_min));
+        const int grid = s->cfg.persistent ? std::min(grid_cap, s->total_tiles) : 0;
+        cudaGraphExec_t ex;
+        rc = chunk_graph(s, len, grid, &ex);
+        if (rc) break;
+        if (cudaGraphLaunch(ex, s->st) != cudaSuccess) {
+            rc = set_error(PTK_ERR_CUDA, "chunk launch failed");
+            break;
+        }
+        count_graph_launch(len + 1);
+        s->launches += len + 1;
+        ++s->chunks;
+        if (cudaStreamSynchronize(s->st) != cudaSuccess) {
+            rc = set_error(PTK_ERR_CUDA, "chunk failed: %s", cudaGetErrorString(cudaGetLastError()));
+            break;
+        }
+        t = clock();
+        std::vector<Inst *> still;
+        for (Inst *in : s->active) {
+            in->done += std::min(len, in->steps_total - in->done);
+            if (in->done >= in->steps_total) {
+                rc = retire(s, in, t);
+                if (rc) break;
+                s->dirty = true;
+            } else {
+                still.push_back(in);
+            }
+        }
+        s->active.swap(still);
+    }
+    s->wall_s += clock();
+    return rc;
+}
+
+int ptk_server_request(ptk_server *s, long long ticket, ptk_request_info *info)
+{
+    PTK_CHECK_ARG(s && info, "NULL argument");
+    if (ticket < 0 || ticket >= (long long)s->all.size()) return set_error(PTK_ERR_NOTFOUND, "no ticket %lld", ticket);
+    Inst *in = s->all[(size_t)ticket];
+    info->ticket = ticket;
+    info->Nx = in->desc.Nx;
+    info->Ny = in->desc.Ny;
+    info->Nz = in->desc.Nz;
+    info->steps = in->desc.steps;
+    info->arrival_s = in->t_arrival;
+    info->admit_s = in->t_admit;
+    info->finish_s = in->t_finish;
+    info->done = in->finished ? 1 : 0;
+    for (int f = 0; f < 6; ++f) info->checksum[f] = in->checksum[f];
+    return PTK_OK;
+}
+
+int ptk_server_fetch(ptk_server *s, long long ticket, float *const fields[6])
+{
+    PTK_CHECK_ARG(s && fields, "NULL argument");
+    if (ticket < 0 || ticket >= (long long)s->all.size()) return set_error(PTK_ERR_NOTFOUND, "no ticket %lld", ticket);
+    Inst *in = s->all[(size_t)ticket];
+    if (!in->finished) return set_error(PTK_ERR_STATE, "request %lld has not finished", ticket);
+    if (in->result[0].empty()) return set_error(PTK_ERR_STATE, "server was created without keep_results");
+    for (int f = 0; f < 6; ++f) memcpy(fields[f], in->result[f].data(), in->result[f].size() * sizeof(float));
+    return PTK_OK;
+}
+
+int ptk_server_stats_get(ptk_server *s, ptk_server_stats *st)
+{
+    PTK_CHECK_ARG(s && st, "NULL argument");
+    std::vector<double> lat;
+    for (Inst *in : s->all)
+        if (in->finished) lat.push_back(in->t_finish - in->t_arrival_run);
+    std::sort(lat.begin(), lat.end());
+    auto pct = [&](double q) {
+        if (lat.empty()) return 0.0;
+        size_t i = (size_t)std::ceil(q * lat.size()) - 1;
+        return lat[std::min(i, lat.size() - 1)];
+    };
+    memset(st, 0, sizeof *st);
+    st->submitted = (long long)s->all.size();
+    st->completed = (long long)lat.size();
+    st->wall_s = s->wall_s;
+    st->solves_per_s = s->wall_s > 0 ? lat.size() / s->wall_s : 0;
+    st->p50_latency_s = pct(0.50);
+    st->p99_latency_s = pct(0.99);
+    double sum = 0;
+    for (double v : lat) sum += v;
+    st->mean_latency_s = lat.empty() ? 0 : sum / lat.size();
+    st->cell_updates = s->cell_updates;
+    st->mcells_per_s = s->wall_s > 0 ? s->cell_updates / s->wall_s / 1e6 : 0;
+    st->chunks = s->chunks;
+    st->kernel_launches = s->launches;
+    st->peak_active = s->peak_active;
+    st->peak_bytes = s->peak_bytes;
+    return PTK_OK;
+}
+
+int ptk_server_destroy(ptk_server *s)
+{
+    if (!s) return PTK_OK;
+    cudaStreamSynchronize(s->st);
+    for (Inst *in : s->active) release(s, in);
+    for (auto &kv : s->graphs) cudaGraphExecDestroy(kv.second);
+    if (s->d_desc) pool_free(s->d_desc, s->st);
+    if (s->d_tile0) pool_free(s->d_tile0, s->st);
+    if (s->h_desc) cudaFreeHost(s->h_desc);
+    if (s->h_tile0) cudaFreeHost(s->h_tile0);
+    cudaStreamSynchronize(s->st);
+    cudaStreamDestroy(s->st);
+    for (Inst *in : s->all) delete in;
+    delete s;
+    return PTK_OK;
+}
+
+}  // extern "C"

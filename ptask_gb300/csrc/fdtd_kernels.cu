@@ -139,28 +139,32 @@ __device__ void yee_faces(const InstDesc *__restrict__ D, int par, int ftile, in
 // ---------------------------------------------------------------------------------------------
 template <int BY>
 __global__ void __launch_bounds__(32 * (BY + 1), BY <= 4 ? 4 : (BY <= 8 ? 2 : 1))
-k_yee_step(const InstDesc *__restrict__ insts, const int *__restrict__ tile0, int ninst, int s_off)
+k_yee_step(const InstDesc *__restrict__ insts, const int *__restrict__ tile0, int ninst, int s_off,
+           int total_tiles)
 {
     __shared__ float4 sEx[BY + 1][32];
     __shared__ float4 sEz[BY + 1][32];
     __shared__ float4 sHx[BY + 1][32];
     __shared__ float4 sHz[BY + 1][32];
 
-    const int t = blockIdx.x;
+    // Persistent form: a CTA takes tiles blockIdx.x, blockIdx.x + gridDim.x, ...  Shared memory is
+    // safe to reuse across tiles: every plane ends with a barrier after the last read of sEx/sEz,
+    // and sHx/sHz are first written after the next tile's first barrier.
+    for (int t = blockIdx.x; t < total_tiles; t += gridDim.x) {
     int lo = 0, hi = ninst;
     while (hi - lo > 1) {
         const int mid = (lo + hi) >> 1;
         if (__ldg(tile0 + mid) <= t) lo = mid; else hi = mid;
     }
     const InstDesc *__restrict__ D = insts + lo;
-    if (s_off >= D->steps_left) return;
+    if (s_off >= D->steps_left) continue;
     const int lt = t - __ldg(tile0 + lo);
     const int step = D->step + s_off;
     const int par = step & 1;
     const int nmain = D->tiles_x * D->tiles_y * D->tiles_z;
     if (lt >= nmain) {
         yee_faces(D, par, lt - nmain, 32 * (BY + 1) * kFaceCellsPerThread);
-        return;
+        continue;
     }
 
     const int nx = D->nx, ny = D->ny, nz = D->nz, pitch = D->pitch, kc = D->kc;
@@ -329,6 +333,7 @@ k_yee_step(const InstDesc *__restrict__ insts, const int *__restrict__ tile0, in
             ey0 = ey1;
         }
     }
+    }   // tile loop
 }
 
 __global__ void k_advance(InstDesc *insts, int ninst, int nsteps)
@@ -357,19 +362,43 @@ void plan_tiles(InstDesc &d, int by, int kc)
     d.face_tiles = (int)((fc + per - 1) / per);
 }
 
-int launch_yee_step(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles,
-                    int s_offset, int by, cudaStream_t s)
+int launch_yee_step_grid(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles,
+                         int s_offset, int by, int grid, cudaStream_t s)
 {
     if (total_tiles <= 0) return PTK_OK;
+    const int g = (grid <= 0 || grid > total_tiles) ? total_tiles : grid;
     switch (by) {
-    case 4: k_yee_step<4><<<total_tiles, dim3(32, 5), 0, s>>>(d_insts, d_tile0, ninst, s_offset); break;
-    case 8: k_yee_step<8><<<total_tiles, dim3(32, 9), 0, s>>>(d_insts, d_tile0, ninst, s_offset); break;
-    case 16: k_yee_step<16><<<total_tiles, dim3(32, 17), 0, s>>>(d_insts, d_tile0, ninst, s_offset); break;
+    case 4: k_yee_step<4><<<g, dim3(32, 5), 0, s>>>(d_insts, d_tile0, ninst, s_offset, total_tiles); break;
+    case 8: k_yee_step<8><<<g, dim3(32, 9), 0, s>>>(d_insts, d_tile0, ninst, s_offset, total_tiles); break;
+    case 16: k_yee_step<16><<<g, dim3(32, 17), 0, s>>>(d_insts, d_tile0, ninst, s_offset, total_tiles); break;
     default: return set_error(PTK_ERR_INVALID, "tile rows must be 4, 8 or 16 (got %d)", by);
     }
     PTK_CUDA_TRY(cudaGetLastError());
     count_launches(1);
     return PTK_OK;
+}
+
+int launch_yee_step(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles,
+                    int s_offset, int by, cudaStream_t s)
+{
+    return launch_yee_step_grid(d_insts, d_tile0, ninst, total_tiles, s_offset, by, 0, s);
+}
+
+int yee_resident_ctas(int by)
+{
+    int per_sm = 0;
+    cudaError_t e = cudaSuccess;
+    switch (by) {
+    case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_yee_step<4>, 32 * 5, 0); break;
+    case 8: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_yee_step<8>, 32 * 9, 0); break;
+    case 16: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_yee_step<16>, 32 * 17, 0); break;
+    default: return 0;
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return per_sm * sm_count();
 }
 
 int launch_advance(InstDesc *d_insts, int ninst, int nsteps, cudaStream_t s)

@@ -7,13 +7,14 @@
 // (splitmix64 stream), so the same arrays come out on x86-64 and aarch64.
 //
 // Must be compiled with -ffp-contract=off: Cb = Dt/(eps0*eps_r) is formed with separately rounded
-// FP32 operations so that a vacuum cell gets exactly the reference's fl(Dt/eps0).
+// FP32 operations so that a vacuum cell gets exactly the reference's fl(Dt/eps0).  The device-side
+// generator (k_generate_coefs in fdtd_batch.cu) evaluates the same expression from the same boxes.
 #include <cmath>
 #include <cstddef>
 #include <cstdint>
 #include <vector>
 
-#include "../../include/ptask_gb300.h"
+#include "ptk_problem.h"
 
 namespace {
 
@@ -54,6 +55,62 @@ void base_params(int Nx, int Ny, int Nz, ptk_fdtd_params *p)
 
 }  // namespace
 
+namespace ptk {
+
+int problem_plan(const ptk_problem_desc *d, ptk_fdtd_params *p, std::vector<BoxSpec> *boxes, int *si, int *sj,
+                 int *sk, std::vector<float> *wave)
+{
+    if (!d || !p || d->Nx < 1 || d->Ny < 1 || d->Nz < 1 || d->steps < 0 || d->n_boxes < 0) return PTK_ERR_INVALID;
+    const int Nx = d->Nx, Ny = d->Ny, Nz = d->Nz;
+    base_params(Nx, Ny, Nz, p);
+    const double cx = p->Cx, cy = p->Cy, cz = p->Cz;
+    p->Dt = (float)((double)d->courant / ((double)p->c0 * std::sqrt(cx * cx + cy * cy + cz * cz)));
+
+    Rng r{d->seed};
+    if (boxes) boxes->clear();
+    for (int b = 0; b < d->n_boxes; ++b) {
+        const int N[3] = {Nx, Ny, Nz};
+        BoxSpec bx;
+        for (int a = 0; a < 3; ++a) {
+            int size = r.range(d->box_min, d->box_max);
+            if (size < 1) size = 1;
+            if (size > N[a]) size = N[a];
+            bx.lo[a] = r.range(0, N[a] - size);
+            bx.hi[a] = bx.lo[a] + size;
+        }
+        bx.epsr = (float)(d->eps_min + (double)(d->eps_max - d->eps_min) * r.u01());
+        if (boxes) boxes->push_back(bx);
+    }
+    int i = -1, j = -1, k = -1;
+    if (d->source_mode != 0 && Nx >= 2 && Ny >= 2) {
+        if (d->source_mode == 1) {
+            i = Nx / 2; j = Ny / 2; k = Nz / 2;
+        } else {
+            i = r.range(1, Nx - 1);
+            j = r.range(1, Ny - 1);
+            k = r.range(0, Nz - 1);
+        }
+    }
+    if (si) *si = i;
+    if (sj) *sj = j;
+    if (sk) *sk = k;
+    if (wave) {
+        // Gaussian pulse exp(-((n - t0)/tw)^2), tw in steps, t0 = 3 tw.
+        wave->assign((size_t)d->steps, 0.0f);
+        double tw = d->steps / 8.0;
+        if (tw > 20.0) tw = 20.0;
+        if (tw < 2.0) tw = 2.0;
+        const double t0 = 3.0 * tw;
+        for (int n = 0; n < d->steps; ++n) {
+            const double a = ((double)n - t0) / tw;
+            (*wave)[(size_t)n] = (i >= 0) ? (float)std::exp(-a * a) : 0.0f;
+        }
+    }
+    return PTK_OK;
+}
+
+}  // namespace ptk
+
 extern "C" {
 
 int ptk_reference_params(int Nx, int Ny, int Nz, ptk_fdtd_params *p)
@@ -73,33 +130,20 @@ int ptk_fill_uniform(float *dst, size_t n, float scale, uint64_t seed)
     return PTK_OK;
 }
 
-int ptk_problem_generate(const ptk_problem_desc *d, ptk_fdtd_params *p, float *Ca, float *Cb,
-                         float *Da, float *Db, int *si, int *sj, int *sk, float *wave)
+int ptk_problem_generate(const ptk_problem_desc *d, ptk_fdtd_params *p, float *Ca, float *Cb, float *Da,
+                         float *Db, int *si, int *sj, int *sk, float *wave)
 {
-    if (!d || !p || d->Nx < 1 || d->Ny < 1 || d->Nz < 1 || d->steps < 0) return PTK_ERR_INVALID;
+    std::vector<ptk::BoxSpec> boxes;
+    std::vector<float> w;
+    int rc = ptk::problem_plan(d, p, &boxes, si, sj, sk, &w);
+    if (rc) return rc;
     const int Nx = d->Nx, Ny = d->Ny, Nz = d->Nz;
-    base_params(Nx, Ny, Nz, p);
-    const double cx = p->Cx, cy = p->Cy, cz = p->Cz;
-    p->Dt = (float)((double)d->courant / ((double)p->c0 * std::sqrt(cx * cx + cy * cy + cz * cz)));
-
-    Rng r{d->seed};
     const size_t ncell = (size_t)Nx * Ny * Nz;
     std::vector<float> epsr(ncell, 1.0f);
-    for (int b = 0; b < d->n_boxes; ++b) {
-        const int N[3] = {Nx, Ny, Nz};
-        int lo[3], hi[3];
-        for (int a = 0; a < 3; ++a) {
-            int size = r.range(d->box_min, d->box_max);
-            if (size < 1) size = 1;
-            if (size > N[a]) size = N[a];
-            lo[a] = r.range(0, N[a] - size);
-            hi[a] = lo[a] + size;
-        }
-        const float e = (float)(d->eps_min + (double)(d->eps_max - d->eps_min) * r.u01());
-        for (int k = lo[2]; k < hi[2]; ++k)
-            for (int j = lo[1]; j < hi[1]; ++j)
-                for (int i = lo[0]; i < hi[0]; ++i) epsr[(size_t)i + (size_t)Nx * j + (size_t)Nx * Ny * k] = e;
-    }
+    for (const ptk::BoxSpec &b : boxes)   // later boxes overwrite earlier ones
+        for (int k = b.lo[2]; k < b.hi[2]; ++k)
+            for (int j = b.lo[1]; j < b.hi[1]; ++j)
+                for (int i = b.lo[0]; i < b.hi[0]; ++i) epsr[(size_t)i + (size_t)Nx * j + (size_t)Nx * Ny * k] = b.epsr;
     const float ch = p->Dt / p->mu0;
     for (size_t c = 0; c < ncell; ++c) {
         if (Ca) Ca[c] = 1.0f;
@@ -107,31 +151,8 @@ int ptk_problem_generate(const ptk_problem_desc *d, ptk_fdtd_params *p, float *C
         if (Da) Da[c] = 1.0f;
         if (Db) Db[c] = ch;
     }
-
-    int i = -1, j = -1, k = -1;
-    if (d->source_mode != 0 && Nx >= 2 && Ny >= 2) {
-        if (d->source_mode == 1) {
-            i = Nx / 2; j = Ny / 2; k = Nz / 2;
-        } else {
-            i = r.range(1, Nx - 1);
-            j = r.range(1, Ny - 1);
-            k = r.range(0, Nz - 1);
-        }
-    }
-    if (si) *si = i;
-    if (sj) *sj = j;
-    if (sk) *sk = k;
-    if (wave) {
-        // Gaussian pulse exp(-((n - t0)/tw)^2), tw in steps, t0 = 3 tw.
-        double tw = d->steps / 8.0;
-        if (tw > 20.0) tw = 20.0;
-        if (tw < 2.0) tw = 2.0;
-        const double t0 = 3.0 * tw;
-        for (int n = 0; n < d->steps; ++n) {
-            const double a = ((double)n - t0) / tw;
-            wave[n] = (i >= 0) ? (float)std::exp(-a * a) : 0.0f;
-        }
-    }
+    if (wave)
+        for (size_t n = 0; n < w.size(); ++n) wave[n] = w[n];
     return PTK_OK;
 }
 

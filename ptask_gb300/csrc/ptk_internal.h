@@ -83,6 +83,11 @@ int face_tile_cells(int by);
 // Launchers (asynchronous on `s`).
 int launch_yee_step(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles,
                     int s_offset, int by, cudaStream_t s);
+// Same, with `grid` CTAs looping over the tiles (0: one CTA per tile).
+int launch_yee_step_grid(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles,
+                         int s_offset, int by, int grid, cudaStream_t s);
+// CTAs of the step kernel with `by` rows that fit on the whole GPU at once.
+int yee_resident_ctas(int by);
 int launch_advance(InstDesc *d_insts, int ninst, int nsteps, cudaStream_t s);
 int launch_pack_field(const float *src, int ex, int ey, int ez, const Layout &L, float *dst0,
                       float *dst1, cudaStream_t s);

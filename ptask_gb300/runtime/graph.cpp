@@ -561,6 +561,14 @@ static Datablock *take_for(Task *t, Port *p)
 
 bool Graph::task_ready(Task *t)
 {
+    // With loop lowering on, the head of a loop does not start an instance task by task before the
+    // loop's iteration count has arrived: once it has, the whole loop is lowered at once.
+    if (t->m_loop_top && m_lower_cycles && !t->m_loop_top->entered) {
+        bool count = false;
+        for (Channel *c : t->m_loop_top->meta->m_in)
+            if (c->GetQueueDepth()) count = true;
+        if (!count) return false;
+    }
     for (Port *p : t->m_inputs) {
         switch (p->GetPortType()) {
         case INPUT_PORT: {

@@ -162,7 +162,13 @@ void *Datablock::GetDataPointer(BOOL bWriteable, BOOL bSynchronizeBufferView)
     if (bSynchronizeBufferView) sync_host();
     ensure_host_alloc();
     if (m_event && m_dev_valid && !m_d2h_pending) ptk_event_sync(m_event);   // pending H2D reads m_host
-    if (bWriteable) m_dev_valid = false;
+    if (bWriteable) {
+        // The caller writes the host view: it becomes the only valid copy.
+        if (m_d2h_pending) ptk_event_sync(m_event);
+        m_d2h_pending = false;
+        m_host_valid = true;
+        m_dev_valid = false;
+    }
     return m_host;
 }
 

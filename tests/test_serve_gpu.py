@@ -1,0 +1,85 @@
+"""Batched and served FDTD: every result is the same alone and in the mix (bit for bit), admission
+respects the HBM budget, and small requests match the oracle."""
+import numpy as np
+import pytest
+
+import oracle
+import ptask_gb300 as P
+from ptask_gb300.serve import Request, Server, batched_instances, poisson_trace
+
+pytestmark = pytest.mark.gpu
+
+
+def alone(r: Request):
+    """The same request solved alone by the single-instance solver."""
+    pr = P.Problem.generate(r.nx, r.ny, r.nz, n_boxes=r.n_boxes, eps=r.eps, box=r.box, steps=r.steps,
+                            source_mode=r.source_mode, seed=r.seed)
+    return P.solve(pr, P.zero_fields(r.nx, r.ny, r.nz), r.steps), pr
+
+
+def test_mixed_batch_results_equal_alone():
+    reqs = [Request(24, 20, 16, 40, 2, 1), Request(37, 29, 23, 75, 3, 2), Request(64, 48, 40, 33, 1, 3),
+            Request(17, 33, 9, 61, 2, 4), Request(130, 24, 20, 20, 4, 5)]
+    with Server(keep_results=True, chunk_steps=16) as s:
+        tickets = [s.submit(r) for r in reqs]
+        s.run(time_scale=0)
+        st = s.stats()
+        assert st["completed"] == len(reqs) and st["peak_active"] == len(reqs)
+        for t, r in zip(tickets, reqs):
+            got = s.fetch(t)
+            ref, _ = alone(r)
+            for q in range(6):
+                np.testing.assert_array_equal(got[q], ref[q], err_msg=f"request {t} field {P.FIELDS[q]}")
+
+
+def test_batched_small_requests_match_oracle():
+    reqs = [Request(20, 18, 14, 30, 2, 11), Request(26, 22, 12, 45, 1, 12)]
+    with Server(keep_results=True, chunk_steps=8, persistent=False) as s:
+        tickets = [s.submit(r) for r in reqs]
+        s.run(time_scale=0)
+        for t, r in zip(tickets, reqs):
+            got = s.fetch(t)
+            _, pr = alone(r)
+            ref = oracle.step_ext_f32(P.zero_fields(r.nx, r.ny, r.nz), r.steps, pr.params, pr.Ca, pr.Cb, pr.Da,
+                                      pr.Db, pr.src, pr.wave)
+            for q in range(6):
+                assert oracle.normwise_error(got[q], ref[q]) <= 1e-5
+                np.testing.assert_array_equal(got[q], ref[q])
+
+
+def test_continuous_admission_within_budget_and_plain_mode_agrees():
+    reqs = poisson_trace(24, rate=400.0, seed=9, edge=(16, 72), steps=(20, 120))
+    # a budget that holds only a few instances at a time
+    budget = 3 * 16 * 4 * (96 * 73 * 73) + (1 << 20)
+    with Server(budget_bytes=budget, keep_results=True, chunk_steps=8) as s:
+        tickets = [s.submit(r) for r in reqs]
+        s.run(time_scale=1.0)
+        st = s.stats()
+        assert st["completed"] == len(reqs)
+        assert st["peak_bytes"] <= budget
+        batched = {t: s.fetch(t) for t in tickets}
+        lat = [s.info(t).finish_s - s.info(t).arrival_s for t in tickets]
+        assert min(lat) >= 0
+    with Server(max_active=1, keep_results=True, chunk_steps=8) as s:
+        tickets = [s.submit(r) for r in reqs]
+        s.run(time_scale=0)
+        assert s.stats()["peak_active"] == 1
+        for t in tickets:
+            got = s.fetch(t)
+            for q in range(6):
+                np.testing.assert_array_equal(got[q], batched[t][q])
+
+
+def test_request_larger_than_budget_is_rejected():
+    with Server(budget_bytes=1 << 20) as s:
+        with pytest.raises(P.PtkError):
+            s.submit(Request(64, 64, 64, 10, 1, 1))
+
+
+def test_batched_config_generator_shapes():
+    reqs = batched_instances(64)
+    assert len(reqs) == 64
+    e = np.array([[r.nx, r.ny, r.nz] for r in reqs])
+    assert e.min() >= 32 and e.max() <= 192
+    assert all(100 <= r.steps <= 2000 for r in reqs)
+    assert all(1 <= r.n_boxes <= 8 for r in reqs)
