@@ -202,6 +202,24 @@ int ptk_fdtd_solve(const ptk_fdtd_params *p, float *const fields[6], const float
                    const float *Cb, const float *Da, const float *Db, int si, int sj, int sk,
                    const float *wave, int nwave, int steps, float *ms);
 
+/* Allocation-free solve.  No counterpart in the reference: it exists for callers that cannot let a
+ * library allocate GPU memory -- code running while another component captures the stream into a CUDA
+ * graph (cudaMalloc is not allowed there), plugins whose host application owns all device memory, and
+ * latency-critical loops that must not risk an allocation failure mid-run.
+ * fields[6] (device, reference layout) are advanced `steps` steps in place with the fused kernel;
+ * Ca..Db (device, Nx*Ny*Nz each) may all be NULL for vacuum coefficients; wave (device) may be NULL.
+ * stream NULL means the current device's default stream.  All scratch lives in one static device
+ * array of ptk_fdtd_static_scratch_bytes() bytes (48 MiB) that every GPU loading the library holds
+ * until exit; grids needing more (padded node count roundup(Nx+1,32)*(Ny+1)*(Nz+1) above about 786k)
+ * are rejected with PTK_ERR_BUDGET.  The first call on a device looks up the array's address
+ * (cudaGetSymbolAddress) with that device current: make it before any stream capture.  Calls share
+ * the array, which keeps the previous call's contents (each call clears what it uses): calls whose
+ * GPU work overlaps race and must be serialised by the caller. */
+int ptk_fdtd_solve_static(const ptk_fdtd_params *p, float *const fields[6], const float *Ca,
+                          const float *Cb, const float *Da, const float *Db, int si, int sj, int sk,
+                          const float *wave, int nwave, int steps, void *stream);
+size_t ptk_fdtd_static_scratch_bytes(void);
+
 /* ============================== batched / served FDTD ========================================= */
 /* Many device-resident FDTD instances of uneven size advanced together: every time step of every
  * active instance is one persistent launch of the fused step kernel over the concatenated tile lists,

@@ -124,6 +124,9 @@ _SIGS = {
     "ptk_solver_last_launches": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "ptk_fdtd_solve": (C.c_int, [C.POINTER(FdtdParams), C.POINTER(_P), _P, _P, _P, _P, C.c_int, C.c_int,
                                  C.c_int, _P, C.c_int, C.c_int, C.POINTER(C.c_float)]),
+    "ptk_fdtd_solve_static": (C.c_int, [C.POINTER(FdtdParams), C.POINTER(_P), _P, _P, _P, _P, C.c_int, C.c_int,
+                                        C.c_int, _P, C.c_int, C.c_int, _P]),
+    "ptk_fdtd_static_scratch_bytes": (C.c_size_t, []),
     "ptk_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(_P)]),
     "ptk_server_submit": (C.c_int, [_P, C.POINTER(ProblemDesc), C.c_double, C.POINTER(C.c_longlong)]),
     "ptk_server_run": (C.c_int, [_P, C.c_double]),
