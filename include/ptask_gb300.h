@@ -161,10 +161,12 @@ int ptk_graph_exec_destroy(void *graph_exec);
 typedef struct ptk_solver ptk_solver;
 
 /* Tile shape of the fused step kernel.  by: rows per CTA (4, 8 or 16); kc: z-planes per CTA (>=1,
- * 0 = whole depth).  Zeroes select the autotuned / default choice. */
+ * 0 = whole depth); vec: x cells per thread (1, 2 or 4; tiles are 32*vec cells wide, 0 = choose
+ * from Nx).  by = kc = 0 selects the default shape. */
 typedef struct ptk_tile_config {
     int by;
     int kc;
+    int vec;
 } ptk_tile_config;
 
 int ptk_solver_create(const ptk_fdtd_params *p, ptk_solver **out);

@@ -112,6 +112,7 @@ struct ptk_server {
     int *h_tile0 = nullptr;
     int cap = 0;
     int total_tiles = 0;
+    int vec = 4;                    // x cells per thread of the current work list
     bool dirty = true;
     std::map<std::tuple<int, int, int, int>, cudaGraphExec_t> graphs;
     long long chunks = 0, launches = 0;
@@ -216,6 +217,26 @@ int rebuild_worklist(ptk_server *s)
     int rc = grow_worklist(s, n);
     if (rc) return rc;
     cudaStreamSynchronize(s->st);   // the pinned staging may still feed a previous copy
+    // x cells per thread for this launch: the widest tile whose share of lanes holding cells
+    // (weighted by the remaining work) is within 10 % of the best width's.
+    double eff[3] = {0, 0, 0}, work = 0;
+    const int vecs[3] = {1, 2, 4};
+    for (Inst *in : s->active) {
+        const double w = (double)in->L.nx * in->L.ny * in->L.nz * (in->steps_total - in->done);
+        work += w;
+        for (int v = 0; v < 3; ++v) {
+            const int tx = 32 * vecs[v];
+            eff[v] += w * in->L.nx / (double)(tx * ((in->L.nx + tx - 1) / tx));
+        }
+    }
+    const double best = std::max(eff[0], std::max(eff[1], eff[2]));
+    s->vec = 1;
+    for (int v = 2; v >= 0; --v)
+        if (eff[v] >= 0.9 * best) {
+            s->vec = vecs[v];
+            break;
+        }
+    (void)work;
     int tiles = 0;
     for (int q = 0; q < n; ++q) {
         Inst *in = s->active[q];
@@ -231,7 +252,7 @@ int rebuild_worklist(ptk_server *s)
         d.nwave = in->nwave;
         d.step = in->done;
         d.steps_left = in->steps_total - in->done;
-        plan_tiles(d, s->cfg.tile_rows, in->L.nz > 48 ? 16 : 0);
+        plan_tiles(d, s->cfg.tile_rows, in->L.nz > 48 ? 16 : 0, s->vec);
         s->h_desc[q] = d;
         s->h_tile0[q] = tiles;
         tiles += d.tiles_x * d.tiles_y * d.tiles_z + d.face_tiles;
@@ -249,7 +270,7 @@ int rebuild_worklist(ptk_server *s)
 int chunk_graph(ptk_server *s, int len, int grid, cudaGraphExec_t *out)
 {
     const int n = (int)s->active.size();
-    auto key = std::make_tuple(len, n, s->total_tiles, grid);
+    auto key = std::make_tuple(len, n, s->total_tiles, grid * 8 + s->vec);
     auto it = s->graphs.find(key);
     if (it != s->graphs.end()) {
         *out = it->second;
@@ -261,7 +282,7 @@ int chunk_graph(ptk_server *s, int len, int grid, cudaGraphExec_t *out)
     set_capturing(true);
     int rc = PTK_OK;
     for (int q = 0; q < len && !rc; ++q)
-        rc = launch_yee_step_grid(s->d_desc, s->d_tile0, n, s->total_tiles, q, s->cfg.tile_rows, grid, cap);
+        rc = launch_yee_step_v(s->d_desc, s->d_tile0, n, s->total_tiles, q, s->cfg.tile_rows, s->vec, grid, cap);
     if (!rc) rc = launch_advance(s->d_desc, n, len, cap);
     set_capturing(false);
     cudaGraph_t g = nullptr;
@@ -374,7 +395,8 @@ int ptk_server_run(ptk_server *s, double time_scale)
     for (Inst *in : order) in->t_arrival_run = time_scale > 0 ? in->t_arrival * time_scale : 0.0;
     const double t0 = now_s();
     size_t nxt = 0;
-    const int grid_cap = std::max(1, yee_resident_ctas(s->cfg.tile_rows));
+    int grid_cap[5] = {0, 0, 0, 0, 0};   // resident CTAs per vec (1, 2, 4)
+    for (int v : {1, 2, 4}) grid_cap[v] = std::max(1, yee_resident_ctas(s->cfg.tile_rows, v));
     auto clock = [&] { return (now_s() - t0); };
     auto arrived = [&](Inst *in, double t) { return time_scale <= 0 || in->t_arrival * time_scale <= t; };
     int rc = PTK_OK;
@@ -404,7 +426,7 @@ int ptk_server_run(ptk_server *s, double time_scale)
         for (Inst *in : s->active) left_min = std::min(left_min, in->steps_total - in->done);
         // chunk length: the configured chunk, shortened so that the first finisher leaves promptly
         const int len = std::max(1, std::min(s->cfg.chunk_steps, left_min));
-        const int grid = s->cfg.persistent ? std::min(grid_cap, s->total_tiles) : 0;
+        const int grid = s->cfg.persistent ? std::min(grid_cap[s->vec], s->total_tiles) : 0;
         cudaGraphExec_t ex;
         rc = chunk_graph(s, len, grid, &ex);
         if (rc) break;

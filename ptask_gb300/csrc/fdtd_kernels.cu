@@ -39,43 +39,50 @@ __device__ __forceinline__ float yee_ref(float h, float c, float a1, float a0, f
     return __fadd_rn(h, __fmul_rn(c, curl));
 }
 
-struct F4 {
-    float v[4];
+// V consecutive x cells held by one thread (V = 1, 2, 4: 32-, 64- or 128-bit accesses).
+template <int V>
+struct __align__(4 * V) Vec {
+    float v[V];
 };
 
-__device__ __forceinline__ F4 ld4(const float *__restrict__ p)
+template <int V>
+__device__ __forceinline__ Vec<V> ldv(const float *__restrict__ p)
 {
-    const float4 t = __ldg(reinterpret_cast<const float4 *>(p));
-    F4 r;
-    r.v[0] = t.x; r.v[1] = t.y; r.v[2] = t.z; r.v[3] = t.w;
+    Vec<V> r;
+    if constexpr (V == 4) {
+        const float4 t = __ldg(reinterpret_cast<const float4 *>(p));
+        r.v[0] = t.x; r.v[1] = t.y; r.v[2] = t.z; r.v[3] = t.w;
+    } else if constexpr (V == 2) {
+        const float2 t = __ldg(reinterpret_cast<const float2 *>(p));
+        r.v[0] = t.x; r.v[1] = t.y;
+    } else {
+        r.v[0] = __ldg(p);
+    }
     return r;
 }
 
-__device__ __forceinline__ F4 zero4()
+template <int V>
+__device__ __forceinline__ Vec<V> zerov()
 {
-    F4 r;
-    r.v[0] = r.v[1] = r.v[2] = r.v[3] = 0.f;
+    Vec<V> r;
+#pragma unroll
+    for (int e = 0; e < V; ++e) r.v[e] = 0.f;
     return r;
 }
 
-// Store the first `n` (1..4) elements of v at p; a full aligned vector store when n == 4.
-__device__ __forceinline__ void st4(float *p, const F4 &v, int n)
+// Store the first `n` (1..V) elements of v at p; one aligned vector store when n == V.
+template <int V>
+__device__ __forceinline__ void stv(float *p, const Vec<V> &v, int n)
 {
-    if (n >= 4) {
-        *reinterpret_cast<float4 *>(p) = make_float4(v.v[0], v.v[1], v.v[2], v.v[3]);
+    if (n >= V) {
+        if constexpr (V == 4) *reinterpret_cast<float4 *>(p) = make_float4(v.v[0], v.v[1], v.v[2], v.v[3]);
+        else if constexpr (V == 2) *reinterpret_cast<float2 *>(p) = make_float2(v.v[0], v.v[1]);
+        else p[0] = v.v[0];
     } else {
 #pragma unroll
-        for (int e = 0; e < 4; ++e)
+        for (int e = 0; e < V; ++e)
             if (e < n) p[e] = v.v[e];
     }
-}
-
-__device__ __forceinline__ float4 as_f4(const F4 &v) { return make_float4(v.v[0], v.v[1], v.v[2], v.v[3]); }
-__device__ __forceinline__ F4 from_f4(const float4 &t)
-{
-    F4 r;
-    r.v[0] = t.x; r.v[1] = t.y; r.v[2] = t.z; r.v[3] = t.w;
-    return r;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -126,26 +133,28 @@ __device__ void yee_faces(const InstDesc *__restrict__ D, int par, int ftile, in
 }
 
 // ---------------------------------------------------------------------------------------------
-// Fused Yee step.  One CTA owns a main tile of 128 (x) by BY (y) cells and a range of z planes
+// Fused Yee step.  One CTA owns a main tile of 32*V (x) by BY (y) cells and a range of z planes
 // [k0, k1); it streams the planes in order, keeping the previous plane's new Hx, Hy and the next
 // plane's Ex, Ey in registers (sliding window), so every array element is read from HBM once per
-// step.  Thread (lane, ty): ty = 1..BY own row y0+ty-1, 4 consecutive x cells per lane (128-bit
+// step.  Thread (lane, ty): ty = 1..BY own row y0+ty-1, V consecutive x cells per lane (V*32-bit
 // loads and stores); ty = 0 is a halo row y0-1 that only recomputes new Hx, Hz for the E update of
 // row y0.  In-plane neighbours: x+1 / x-1 through warp shuffles (lane 31 / lane 0 fetch the one
 // cell beyond the tile), y+1 / y-1 through shared memory.  A tile that starts at k0 > 0 first
 // recomputes new Hx, Hy on plane k0-1 ("warm" plane, no stores).
 // Work list: blockIdx.x indexes the concatenated tiles of all instances (tile0 = prefix sums);
-// each instance's main tiles are followed by its face tiles.
+// each instance's main tiles are followed by its face tiles.  Every instance of a launch must have
+// been planned with vec == V.
 // ---------------------------------------------------------------------------------------------
-template <int BY>
+template <int BY, int V>
 __global__ void __launch_bounds__(32 * (BY + 1), BY <= 4 ? 4 : (BY <= 8 ? 2 : 1))
 k_yee_step(const InstDesc *__restrict__ insts, const int *__restrict__ tile0, int ninst, int s_off,
            int total_tiles)
 {
-    __shared__ float4 sEx[BY + 1][32];
-    __shared__ float4 sEz[BY + 1][32];
-    __shared__ float4 sHx[BY + 1][32];
-    __shared__ float4 sHz[BY + 1][32];
+    constexpr int TX = 32 * V;
+    __shared__ Vec<V> sEx[BY + 1][32];
+    __shared__ Vec<V> sEz[BY + 1][32];
+    __shared__ Vec<V> sHx[BY + 1][32];
+    __shared__ Vec<V> sHz[BY + 1][32];
 
     // Persistent form: a CTA takes tiles blockIdx.x, blockIdx.x + gridDim.x, ...  Shared memory is
     // safe to reuse across tiles: every plane ends with a barrier after the last read of sEx/sEz,
@@ -193,55 +202,55 @@ k_yee_step(const InstDesc *__restrict__ insts, const int *__restrict__ tile0, in
     const int xt = r % D->tiles_x; r /= D->tiles_x;
     const int yt = r % D->tiles_y;
     const int zt = r / D->tiles_y;
-    const int x0 = xt * kTileX, y0 = yt * BY;
+    const int x0 = xt * TX, y0 = yt * BY;
     const int k0 = zt * kc, k1 = min(k0 + kc, nz);
     const int kstart = k0 > 0 ? k0 - 1 : k0;
 
     const int lane = threadIdx.x, ty = threadIdx.y;
-    const int i = x0 + 4 * lane;
+    const int i = x0 + V * lane;
     const int j = y0 + ty - 1;
     const bool halo = (ty == 0);
     const bool xin = (i <= nx);               // vector holds at least one node of the row
     const bool jrow = (j >= 0 && j < ny);     // a row of cells (or a valid halo row)
     const bool jshare = (!halo && j == ny);   // the wall row: only lends Ex, Ez to row Ny-1
-    const int nout = min(4, nx - i);          // cells of this vector inside [0, Nx)
-    const bool xl = (lane == 31) && (x0 + kTileX <= nx);   // one node beyond the tile exists
+    const int nout = min(V, nx - i);          // cells of this vector inside [0, Nx)
+    const bool xl = (lane == 31) && (x0 + TX <= nx);   // one node beyond the tile exists
     const bool hcol = (!halo) && (lane == 0) && (x0 > 0) && jrow;   // lane 0 recomputes x0-1
 
     // Offsets are formed only for rows that exist (j >= 0).
     long long off = (long long)i + (long long)pitch * (j < 0 ? 0 : j) + plane * kstart;
 
-    F4 ex0 = zero4(), ey0 = zero4();   // Ex(k), Ey(k)
-    F4 hxp = zero4(), hyp = zero4();   // new Hx, Hy on plane k-1
+    Vec<V> ex0 = zerov<V>(), ey0 = zerov<V>();   // Ex(k), Ey(k)
+    Vec<V> hxp = zerov<V>(), hyp = zerov<V>();   // new Hx, Hy on plane k-1
     if (!halo && xin) {
-        if (jrow || jshare) ex0 = ld4(Ex + off);
-        if (jrow) ey0 = ld4(Ey + off);
+        if (jrow || jshare) ex0 = ldv<V>(Ex + off);
+        if (jrow) ey0 = ldv<V>(Ey + off);
     }
 
     for (int k = kstart; k < k1; ++k, off += plane) {
         const bool warm = (k < k0);
-        F4 hx = zero4(), hy = zero4(), hz = zero4(), ez = zero4(), ex1 = zero4(), ey1 = zero4();
-        F4 da = zero4(), db = zero4(), ca = zero4(), cb = zero4();
-        F4 exj1 = zero4(), ezj1 = zero4();
-        float ez_l = 0.f, ey_l = 0.f;                                  // lane 31: x0+128
+        Vec<V> hx = zerov<V>(), hy = zerov<V>(), hz = zerov<V>(), ez = zerov<V>(), ex1 = zerov<V>(), ey1 = zerov<V>();
+        Vec<V> da = zerov<V>(), db = zerov<V>(), ca = zerov<V>(), cb = zerov<V>();
+        Vec<V> exj1 = zerov<V>(), ezj1 = zerov<V>();
+        float ez_l = 0.f, ey_l = 0.f;                                  // lane 31: x0+TX
         float hy_h = 0.f, hz_h = 0.f, ez_h = 0.f, ex_h0 = 0.f, ex_h1 = 0.f, ex_hj = 0.f,
               ey_h = 0.f, da_h = 0.f, db_h = 0.f;                        // lane 0: x0-1
 
         // ---- loads ----------------------------------------------------------------------
         if (halo) {
             if (!warm && jrow && xin) {
-                hx = ld4(Hx + off); hz = ld4(Hz + off); ez = ld4(Ez + off);
-                ex0 = ld4(Ex + off); ey0 = ld4(Ey + off); ey1 = ld4(Ey + off + plane);
-                da = ld4(Da + off); db = ld4(Db + off);
-                if (xl) ey_l = __ldg(Ey + off + 4);
+                hx = ldv<V>(Hx + off); hz = ldv<V>(Hz + off); ez = ldv<V>(Ez + off);
+                ex0 = ldv<V>(Ex + off); ey0 = ldv<V>(Ey + off); ey1 = ldv<V>(Ey + off + plane);
+                da = ldv<V>(Da + off); db = ldv<V>(Db + off);
+                if (xl) ey_l = __ldg(Ey + off + V);
             }
         } else if (jrow && xin) {
-            hx = ld4(Hx + off); hy = ld4(Hy + off); ez = ld4(Ez + off);
-            ex1 = ld4(Ex + off + plane); ey1 = ld4(Ey + off + plane);
-            da = ld4(Da + off); db = ld4(Db + off);
-            if (!warm) { hz = ld4(Hz + off); ca = ld4(Ca + off); cb = ld4(Cb + off); }
-            if (ty == BY) { exj1 = ld4(Ex + off + pitch); ezj1 = ld4(Ez + off + pitch); }
-            if (xl) { ez_l = __ldg(Ez + off + 4); ey_l = __ldg(Ey + off + 4); }
+            hx = ldv<V>(Hx + off); hy = ldv<V>(Hy + off); ez = ldv<V>(Ez + off);
+            ex1 = ldv<V>(Ex + off + plane); ey1 = ldv<V>(Ey + off + plane);
+            da = ldv<V>(Da + off); db = ldv<V>(Db + off);
+            if (!warm) { hz = ldv<V>(Hz + off); ca = ldv<V>(Ca + off); cb = ldv<V>(Cb + off); }
+            if (ty == BY) { exj1 = ldv<V>(Ex + off + pitch); ezj1 = ldv<V>(Ez + off + pitch); }
+            if (xl) { ez_l = __ldg(Ez + off + V); ey_l = __ldg(Ey + off + V); }
             if (hcol && !warm) {
                 const long long oh = off - 1;
                 hy_h = __ldg(Hy + oh); hz_h = __ldg(Hz + oh); ez_h = __ldg(Ez + oh);
@@ -249,16 +258,16 @@ k_yee_step(const InstDesc *__restrict__ insts, const int *__restrict__ tile0, in
                 ey_h = __ldg(Ey + oh); da_h = __ldg(Da + oh); db_h = __ldg(Db + oh);
             }
         } else if (jshare && xin) {
-            ex0 = ld4(Ex + off); ez = ld4(Ez + off);
+            ex0 = ldv<V>(Ex + off); ez = ldv<V>(Ez + off);
         }
 
         // ---- share Ex, Ez of each row with the row above (its y+1 neighbour) -----------------
-        sEx[ty][lane] = as_f4(ex0);
-        sEz[ty][lane] = as_f4(ez);
+        sEx[ty][lane] = ex0;
+        sEz[ty][lane] = ez;
         __syncthreads();
         if (ty < BY) {
-            exj1 = from_f4(sEx[ty + 1][lane]);
-            ezj1 = from_f4(sEz[ty + 1][lane]);
+            exj1 = sEx[ty + 1][lane];
+            ezj1 = sEz[ty + 1][lane];
         }
 
         // ---- x+1 neighbours through shuffles ----------------------------------------------
@@ -267,11 +276,11 @@ k_yee_step(const InstDesc *__restrict__ insts, const int *__restrict__ tile0, in
         if (lane == 31) { ez_n = ez_l; ey_n = ey_l; }
 
         // ---- new H on plane k ---------------------------------------------------------------
-        F4 hxn, hyn, hzn;
+        Vec<V> hxn, hyn, hzn;
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            const float ez_ip = e < 3 ? ez.v[e + 1] : ez_n;
-            const float ey_ip = e < 3 ? ey0.v[e + 1] : ey_n;
+        for (int e = 0; e < V; ++e) {
+            const float ez_ip = e < V - 1 ? ez.v[e + 1] : ez_n;
+            const float ey_ip = e < V - 1 ? ey0.v[e + 1] : ey_n;
             hxn.v[e] = yee(da.v[e], hx.v[e], db.v[e], ey1.v[e], ey0.v[e], cz, ezj1.v[e], ez.v[e], cy);
             hyn.v[e] = yee(da.v[e], hy.v[e], db.v[e], ez_ip, ez.v[e], cx, ex1.v[e], ex0.v[e], cz);
             hzn.v[e] = yee(da.v[e], hz.v[e], db.v[e], exj1.v[e], ex0.v[e], cy, ey_ip, ey0.v[e], cx);
@@ -284,23 +293,23 @@ k_yee_step(const InstDesc *__restrict__ insts, const int *__restrict__ tile0, in
         }
 
         if (!warm) {
-            sHx[ty][lane] = as_f4(hxn);
-            sHz[ty][lane] = as_f4(hzn);
+            sHx[ty][lane] = hxn;
+            sHz[ty][lane] = hzn;
         }
         __syncthreads();
 
         // ---- x-1 neighbours of new Hy, Hz ---------------------------------------------------
-        float hy_p = __shfl_up_sync(FULL_MASK, hyn.v[3], 1);
-        float hz_p = __shfl_up_sync(FULL_MASK, hzn.v[3], 1);
+        float hy_p = __shfl_up_sync(FULL_MASK, hyn.v[V - 1], 1);
+        float hz_p = __shfl_up_sync(FULL_MASK, hzn.v[V - 1], 1);
         if (lane == 0) { hy_p = hyh; hz_p = hzh; }
 
         if (!halo && jrow && xin) {
             if (!warm) {
-                const F4 hxj = from_f4(sHx[ty - 1][lane]);   // new Hx at j-1
-                const F4 hzj = from_f4(sHz[ty - 1][lane]);   // new Hz at j-1
-                F4 exn, eyn, ezn;
+                const Vec<V> hxj = sHx[ty - 1][lane];   // new Hx at j-1
+                const Vec<V> hzj = sHz[ty - 1][lane];   // new Hz at j-1
+                Vec<V> exn, eyn, ezn;
 #pragma unroll
-                for (int e = 0; e < 4; ++e) {
+                for (int e = 0; e < V; ++e) {
                     const int x = i + e;
                     const float hy_im = e > 0 ? hyn.v[e - 1] : hy_p;
                     const float hz_im = e > 0 ? hzn.v[e - 1] : hz_p;
@@ -316,15 +325,15 @@ k_yee_step(const InstDesc *__restrict__ insts, const int *__restrict__ tile0, in
                 }
                 if (src >= 0) {
                     const long long dsrc = src - off;
-                    if (dsrc >= 0 && dsrc < 4) {
+                    if (dsrc >= 0 && dsrc < V) {
 #pragma unroll
-                        for (int e = 0; e < 4; ++e)
+                        for (int e = 0; e < V; ++e)
                             if (e == (int)dsrc) ezn.v[e] = __fadd_rn(ezn.v[e], srcv);
                     }
                 }
                 if (nout > 0) {
-                    st4(oHx + off, hxn, nout); st4(oHy + off, hyn, nout); st4(oHz + off, hzn, nout);
-                    st4(oEx + off, exn, nout); st4(oEy + off, eyn, nout); st4(oEz + off, ezn, nout);
+                    stv<V>(oHx + off, hxn, nout); stv<V>(oHy + off, hyn, nout); stv<V>(oHz + off, hzn, nout);
+                    stv<V>(oEx + off, exn, nout); stv<V>(oEy + off, eyn, nout); stv<V>(oEz + off, ezn, nout);
                 }
             }
             hxp = hxn;
@@ -350,11 +359,13 @@ __global__ void k_advance(InstDesc *insts, int ninst, int nsteps)
 
 int face_tile_cells(int by) { return 32 * (by + 1) * kFaceCellsPerThread; }
 
-void plan_tiles(InstDesc &d, int by, int kc)
+void plan_tiles(InstDesc &d, int by, int kc, int vec)
 {
     const int kcc = (kc <= 0 || kc > d.nz) ? d.nz : kc;
+    const int tx = 32 * vec;
+    d.vec = vec;
     d.kc = kcc;
-    d.tiles_x = (d.nx + kTileX - 1) / kTileX;
+    d.tiles_x = (d.nx + tx - 1) / tx;
     d.tiles_y = (d.ny + by - 1) / by;
     d.tiles_z = (d.nz + kcc - 1) / kcc;
     const long long fc = (long long)d.ny * d.nz + (long long)d.nx * d.nz + (long long)d.nx * d.ny;
@@ -362,38 +373,58 @@ void plan_tiles(InstDesc &d, int by, int kc)
     d.face_tiles = (int)((fc + per - 1) / per);
 }
 
-int launch_yee_step_grid(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles,
-                         int s_offset, int by, int grid, cudaStream_t s)
+void plan_tiles(InstDesc &d, int by, int kc) { plan_tiles(d, by, kc, 4); }
+
+template <int BY, int V>
+static void launch_by_v(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles, int s_offset,
+                        int g, cudaStream_t s)
+{
+    k_yee_step<BY, V><<<g, dim3(32, BY + 1), 0, s>>>(d_insts, d_tile0, ninst, s_offset, total_tiles);
+}
+
+int launch_yee_step_v(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles, int s_offset,
+                      int by, int vec, int grid, cudaStream_t s)
 {
     if (total_tiles <= 0) return PTK_OK;
     const int g = (grid <= 0 || grid > total_tiles) ? total_tiles : grid;
-    switch (by) {
-    case 4: k_yee_step<4><<<g, dim3(32, 5), 0, s>>>(d_insts, d_tile0, ninst, s_offset, total_tiles); break;
-    case 8: k_yee_step<8><<<g, dim3(32, 9), 0, s>>>(d_insts, d_tile0, ninst, s_offset, total_tiles); break;
-    case 16: k_yee_step<16><<<g, dim3(32, 17), 0, s>>>(d_insts, d_tile0, ninst, s_offset, total_tiles); break;
-    default: return set_error(PTK_ERR_INVALID, "tile rows must be 4, 8 or 16 (got %d)", by);
+#define PTK_CASE(B, W)                                                                       \
+    if (by == B && vec == W) {                                                               \
+        launch_by_v<B, W>(d_insts, d_tile0, ninst, total_tiles, s_offset, g, s);             \
+        PTK_CUDA_TRY(cudaGetLastError());                                                    \
+        count_launches(1);                                                                   \
+        return PTK_OK;                                                                       \
     }
-    PTK_CUDA_TRY(cudaGetLastError());
-    count_launches(1);
-    return PTK_OK;
+    PTK_CASE(4, 1) PTK_CASE(4, 2) PTK_CASE(4, 4)
+    PTK_CASE(8, 1) PTK_CASE(8, 2) PTK_CASE(8, 4)
+    PTK_CASE(16, 1) PTK_CASE(16, 2) PTK_CASE(16, 4)
+#undef PTK_CASE
+    return set_error(PTK_ERR_INVALID, "tile rows must be 4, 8 or 16 and cells per thread 1, 2 or 4 (got %d, %d)",
+                     by, vec);
+}
+
+int launch_yee_step_grid(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles,
+                         int s_offset, int by, int grid, cudaStream_t s)
+{
+    return launch_yee_step_v(d_insts, d_tile0, ninst, total_tiles, s_offset, by, 4, grid, s);
 }
 
 int launch_yee_step(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles,
                     int s_offset, int by, cudaStream_t s)
 {
-    return launch_yee_step_grid(d_insts, d_tile0, ninst, total_tiles, s_offset, by, 0, s);
+    return launch_yee_step_v(d_insts, d_tile0, ninst, total_tiles, s_offset, by, 4, 0, s);
 }
 
-int yee_resident_ctas(int by)
+int yee_resident_ctas(int by, int vec)
 {
     int per_sm = 0;
-    cudaError_t e = cudaSuccess;
-    switch (by) {
-    case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_yee_step<4>, 32 * 5, 0); break;
-    case 8: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_yee_step<8>, 32 * 9, 0); break;
-    case 16: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_yee_step<16>, 32 * 17, 0); break;
-    default: return 0;
-    }
+    cudaError_t e = cudaErrorInvalidValue;
+#define PTK_OCC(B, W)                                                                               \
+    if (by == B && vec == W)                                                                        \
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_yee_step<B, W>, 32 * (B + 1), 0);
+    PTK_OCC(4, 1) PTK_OCC(4, 2) PTK_OCC(4, 4)
+    PTK_OCC(8, 1) PTK_OCC(8, 2) PTK_OCC(8, 4)
+    PTK_OCC(16, 1) PTK_OCC(16, 2) PTK_OCC(16, 4)
+#undef PTK_OCC
     if (e != cudaSuccess) {
         cudaGetLastError();
         return 0;
@@ -401,14 +432,7 @@ int yee_resident_ctas(int by)
     return per_sm * sm_count();
 }
 
-int launch_advance(InstDesc *d_insts, int ninst, int nsteps, cudaStream_t s)
-{
-    if (ninst <= 0) return PTK_OK;
-    k_advance<<<(ninst + 127) / 128, 128, 0, s>>>(d_insts, ninst, nsteps);
-    PTK_CUDA_TRY(cudaGetLastError());
-    count_launches(1);
-    return PTK_OK;
-}
+int yee_resident_ctas(int by) { return yee_resident_ctas(by, 4); }
 
 // ---------------------------------------------------------------------------------------------
 // Layout conversion.

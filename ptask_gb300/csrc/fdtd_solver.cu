@@ -35,11 +35,21 @@ static int store_desc(InstDesc *d_dst, const InstDesc &v, cudaStream_t s)
     return PTK_OK;
 }
 
+// x cells per thread for a row of nx cells: the widest tile that keeps most lanes busy.
+int default_vec(int nx)
+{
+    if (nx >= 96) return 4;
+    if (nx >= 40) return 2;
+    return 1;
+}
+
 // Default tile shape: rows of 8, z depth chosen so the grid holds several waves of CTAs.
-static void default_tiles(int nx, int ny, int nz, int *by, int *kc)
+static void default_tiles(int nx, int ny, int nz, int *by, int *kc, int *vec)
 {
     *by = 8;
-    const long long cols = (long long)((nx + kTileX - 1) / kTileX) * ((ny + 7) / 8);
+    *vec = default_vec(nx);
+    const int tx = 32 * *vec;
+    const long long cols = (long long)((nx + tx - 1) / tx) * ((ny + 7) / 8);
     const long long want = 4LL * std::max(1, sm_count()) * 2;   // ~4 waves at 2 CTAs per SM
     long long zc = (want + cols - 1) / std::max(1LL, cols);
     int k = (int)((nz + zc - 1) / std::max(1LL, zc));
@@ -49,10 +59,10 @@ static void default_tiles(int nx, int ny, int nz, int *by, int *kc)
 }
 
 struct GraphKey {
-    int len, by, kc;
+    int len, by, kc, vec;
     bool operator<(const GraphKey &o) const
     {
-        return std::tie(len, by, kc) < std::tie(o.len, o.by, o.kc);
+        return std::tie(len, by, kc, vec) < std::tie(o.len, o.by, o.kc, o.vec);
     }
 };
 
@@ -69,7 +79,7 @@ struct ptk_solver {
     int nwave = 0;
     long long src = -1;
     int step = 0;              // host mirror of the device step counter
-    int by = 0, kc = 0;
+    int by = 0, kc = 0, vec = 4;
     int total_tiles = 0;
     InstDesc *d_desc = nullptr;
     int *d_tile0 = nullptr;
@@ -95,7 +105,7 @@ static InstDesc host_desc(const ptk_solver *s, int steps_left)
     d.nwave = s->nwave;
     d.step = s->step;
     d.steps_left = steps_left;
-    plan_tiles(d, s->by, s->kc);
+    plan_tiles(d, s->by, s->kc, s->vec);
     return d;
 }
 
@@ -120,7 +130,7 @@ static void drop_graphs(ptk_solver *s)
 // Graph of `len` fused steps + one advance for this solver's current tile shape.
 static int solver_graph(ptk_solver *s, int len, cudaGraphExec_t *out)
 {
-    GraphKey key{len, s->by, s->kc};
+    GraphKey key{len, s->by, s->kc, s->vec};
     auto it = s->graphs.find(key);
     if (it != s->graphs.end()) {
         *out = it->second;
@@ -131,7 +141,7 @@ static int solver_graph(ptk_solver *s, int len, cudaGraphExec_t *out)
     set_capturing(true);
     int rc = PTK_OK;
     for (int q = 0; q < len && rc == PTK_OK; ++q)
-        rc = launch_yee_step(s->d_desc, s->d_tile0, 1, s->total_tiles, q, s->by, s->cap);
+        rc = launch_yee_step_v(s->d_desc, s->d_tile0, 1, s->total_tiles, q, s->by, s->vec, 0, s->cap);
     if (rc == PTK_OK) rc = launch_advance(s->d_desc, 1, len, s->cap);
     set_capturing(false);
     cudaGraph_t g = nullptr;
@@ -207,7 +217,7 @@ int ptk_solver_create(const ptk_fdtd_params *p, ptk_solver **out)
     ptk_solver *s = new ptk_solver();
     s->p = *p;
     s->L = make_layout(p->Nx, p->Ny, p->Nz);
-    default_tiles(p->Nx, p->Ny, p->Nz, &s->by, &s->kc);
+    default_tiles(p->Nx, p->Ny, p->Nz, &s->by, &s->kc, &s->vec);
     cudaStream_t st = default_stream();
     const size_t bytes = (size_t)s->L.total * sizeof(float);
     for (int b = 0; b < 2 && rc == PTK_OK; ++b)
@@ -394,17 +404,20 @@ int ptk_solver_set_tiles(ptk_solver *s, const ptk_tile_config *cfg)
 {
     PTK_CHECK_ARG(s && cfg, "NULL argument");
     std::lock_guard<std::mutex> lk(s->mu);
-    int by = cfg->by, kc = cfg->kc;
+    int by = cfg->by, kc = cfg->kc, vec = cfg->vec;
     if (by == 0 && kc == 0) {
-        default_tiles(s->p.Nx, s->p.Ny, s->p.Nz, &by, &kc);
+        int dv = 4;
+        default_tiles(s->p.Nx, s->p.Ny, s->p.Nz, &by, &kc, &dv);
+        if (vec == 0) vec = dv;
     }
+    if (vec == 0) vec = default_vec(s->p.Nx);
     PTK_CHECK_ARG(by == 4 || by == 8 || by == 16, "tile rows must be 4, 8 or 16 (got %d)", by);
+    PTK_CHECK_ARG(vec == 1 || vec == 2 || vec == 4, "cells per thread must be 1, 2 or 4 (got %d)", vec);
     PTK_CHECK_ARG(kc >= 0, "tile depth must be >= 0");
     if (kc >= s->p.Nz) kc = 0;
-    if (by != s->by || kc != s->kc) {
-        s->by = by;
-        s->kc = kc;
-    }
+    s->by = by;
+    s->kc = kc;
+    s->vec = vec;
     return PTK_OK;
 }
 
@@ -413,6 +426,7 @@ int ptk_solver_get_tiles(const ptk_solver *s, ptk_tile_config *cfg)
     PTK_CHECK_ARG(s && cfg, "NULL argument");
     cfg->by = s->by;
     cfg->kc = s->kc;
+    cfg->vec = s->vec;
     return PTK_OK;
 }
 
@@ -536,11 +550,14 @@ int ptk_autotune_tiles(int Nx, int Ny, int Nz, ptk_tile_config *best, float *bes
     const long long cells = (long long)Nx * Ny * Nz;
     const int steps = (int)std::max(4LL, std::min(64LL, 400000000LL / std::max(1LL, cells)));
     float best_t = 1e30f;
-    ptk_tile_config bc{8, 0};
-    for (int by : rows) {
-        for (int kc : depths) {
+    ptk_tile_config bc{8, 0, default_vec(Nx)};
+    const int vecs[3] = {1, 2, 4};
+    for (int vi = 0; vi < 3 * 3 * 6 && !rc; ++vi) {
+        const int vec = vecs[vi / 18], by = rows[(vi / 6) % 3], kc = depths[vi % 6];
+        {
             if (kc != 0 && kc >= Nz) continue;
-            ptk_tile_config c{by, kc};
+            if (32 * vec > 2 * std::max(Nx, 32)) continue;   // tiles far wider than the grid
+            ptk_tile_config c{by, kc, vec};
             if (ptk_solver_set_tiles(s, &c)) continue;
             if (ptk_solver_run(s, 2, st)) { rc = PTK_ERR_CUDA; break; }
             cudaEventRecord(e0, st);
@@ -555,7 +572,6 @@ int ptk_autotune_tiles(int Nx, int Ny, int Nz, ptk_tile_config *best, float *bes
                 bc = c;
             }
         }
-        if (rc) break;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

@@ -69,14 +69,16 @@ struct InstDesc {
     int steps_left;            // steps still to run at the start of the current chunk
     int tiles_x, tiles_y, tiles_z, face_tiles;
     int kc;                    // z-planes per main tile
-    int pad_;
+    int vec;                   // x cells per thread: main tiles are 32*vec cells wide
 };
 
 // Shape of the fused step kernel's main tiles (x width is fixed at 128 cells).
 constexpr int kTileX = 128;
 constexpr int kFaceCellsPerThread = 4;
 
-// Work-list geometry for an instance under tile rows `by` and depth `kc`.
+// Work-list geometry for an instance under tile rows `by`, depth `kc` and `vec` x cells per thread
+// (the three-argument form plans 128-wide tiles, vec = 4).
+void plan_tiles(InstDesc &d, int by, int kc, int vec);
 void plan_tiles(InstDesc &d, int by, int kc);
 int face_tile_cells(int by);
 
@@ -86,8 +88,12 @@ int launch_yee_step(const InstDesc *d_insts, const int *d_tile0, int ninst, int 
 // Same, with `grid` CTAs looping over the tiles (0: one CTA per tile).
 int launch_yee_step_grid(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles,
                          int s_offset, int by, int grid, cudaStream_t s);
-// CTAs of the step kernel with `by` rows that fit on the whole GPU at once.
+// Same, for tiles planned with `vec` x cells per thread.
+int launch_yee_step_v(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles, int s_offset,
+                      int by, int vec, int grid, cudaStream_t s);
+// CTAs of the step kernel with `by` rows (and `vec`) that fit on the whole GPU at once.
 int yee_resident_ctas(int by);
+int yee_resident_ctas(int by, int vec);
 int launch_advance(InstDesc *d_insts, int ninst, int nsteps, cudaStream_t s);
 int launch_pack_field(const float *src, int ex, int ey, int ez, const Layout &L, float *dst0,
                       float *dst1, cudaStream_t s);

@@ -150,13 +150,15 @@ class Solver:
     def set_vacuum(self, stream=None) -> None:
         call("ptk_solver_set_vacuum", self._h, stream)
 
-    def set_tiles(self, by: int, kc: int) -> None:
-        call("ptk_solver_set_tiles", self._h, C.byref(TileConfig(by, kc)))
+    def set_tiles(self, by: int, kc: int, vec: int = 0) -> None:
+        """Fused-kernel tile shape: `by` rows, `kc` z-planes (0 = all), `vec` x cells per thread
+        (1, 2, 4; 0 = chosen from Nx)."""
+        call("ptk_solver_set_tiles", self._h, C.byref(TileConfig(by, kc, vec)))
 
-    def tiles(self) -> tuple[int, int]:
+    def tiles(self) -> tuple[int, int, int]:
         t = TileConfig()
         call("ptk_solver_get_tiles", self._h, C.byref(t))
-        return t.by, t.kc
+        return t.by, t.kc, t.vec
 
     def reset_clock(self) -> None:
         call("ptk_solver_reset_clock", self._h, None)
@@ -209,9 +211,10 @@ __all__ = ["FIELDS", "Problem", "Solver", "solve", "field_extents", "field_shape
            "random_fields", "reference_params", "launch_count", "device_info", "PTK_HOST", "PTK_DEVICE"]
 
 
-def tuned_tiles(nx: int, ny: int, nz: int) -> tuple[int, int]:
-    """Fastest (rows, z depth) of the fused step kernel for this grid (autotuned, cached per process)."""
+def tuned_tiles(nx: int, ny: int, nz: int) -> tuple[int, int, int]:
+    """Fastest (rows, z depth, x cells per thread) of the fused step kernel for this grid
+    (autotuned on the device, cached per process)."""
     t = TileConfig()
     ms = C.c_float()
     call("ptk_autotune_tiles", nx, ny, nz, C.byref(t), C.byref(ms))
-    return t.by, t.kc
+    return t.by, t.kc, t.vec

@@ -112,17 +112,18 @@ def test_solver_reference_mode_bitwise(shape):
 
 @pytest.mark.parametrize("by", [4, 8, 16])
 @pytest.mark.parametrize("kc", [0, 1, 3, 16])
-def test_tile_shapes_agree(by, kc):
+@pytest.mark.parametrize("vec", [1, 2, 4])
+def test_tile_shapes_agree(by, kc, vec):
     shape, steps = (150, 37, 21), 5
     pr = P.Problem.generate(*shape, n_boxes=3, eps=(1, 10), box=(5, 30), steps=steps, seed=4)
     f = P.random_fields(*shape, seed=32, scale=1e-2)
     ref = oracle.step_ext_f32(f, steps, pr.params, pr.Ca, pr.Cb, pr.Da, pr.Db, pr.src, pr.wave)
     with P.Solver(pr.params) as s:
-        s.set_tiles(by, kc)
+        s.set_tiles(by, kc, vec)
         s.set_fields(f)
         s.set_problem(pr)
         s.run(steps)
-        assert_parity(s.get_fields(), ref, f"tiles by={by} kc={kc}")
+        assert_parity(s.get_fields(), ref, f"tiles by={by} kc={kc} vec={vec}")
 
 
 @pytest.mark.parametrize("shape,boxes,steps", [((32, 32, 32), 2, 100), ((48, 40, 36), 8, 120),
@@ -226,7 +227,7 @@ def test_full_size_tiling_and_chunking_invariance(full_problem):
         s.set_fields(f)
         s.set_problem(pr)
         s.run(333)
-        s.set_tiles(16, 0)
+        s.set_tiles(16, 0, 2)
         s.run(667)
         b = s.get_fields()
     for x, y in zip(a, b):
