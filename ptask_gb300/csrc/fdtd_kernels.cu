@@ -434,6 +434,15 @@ int yee_resident_ctas(int by, int vec)
 
 int yee_resident_ctas(int by) { return yee_resident_ctas(by, 4); }
 
+int launch_advance(InstDesc *d_insts, int ninst, int nsteps, cudaStream_t s)
+{
+    if (ninst <= 0) return PTK_OK;
+    k_advance<<<(ninst + 127) / 128, 128, 0, s>>>(d_insts, ninst, nsteps);
+    PTK_CUDA_TRY(cudaGetLastError());
+    count_launches(1);
+    return PTK_OK;
+}
+
 // ---------------------------------------------------------------------------------------------
 // Layout conversion.
 // ---------------------------------------------------------------------------------------------
