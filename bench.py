@@ -236,7 +236,7 @@ def run_ours(args, wl, world, rank, local):
                               source_mode=1, seed=2 + rank)
     cells = nx * ny * nz
     tiles = None
-    if args.tiles:
+    if args.tiles:   # ROWS,DEPTH[,VEC[,STAGES]]
         tiles = tuple(int(v) for v in args.tiles.split(","))
     elif not args.no_autotune:
         tiles = P.tuned_tiles(nx, ny, nz)
@@ -320,7 +320,7 @@ def run_ours(args, wl, world, rank, local):
     peak, peak_src = hbm_peak()
     achieved = BYTES_PER_CELL * cells / (per_launch_ms / 1e3) / 1e9
     tpc = traffic_per_cell()
-    by, kc, vec = solver.tiles()
+    by, kc, vec, stages = solver.tiles()
     line = {
         "metric": "FDTD Mcell-updates/s", "value": value, "unit": "Mcell-updates/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
@@ -329,7 +329,8 @@ def run_ours(args, wl, world, rank, local):
         "config": {"workload": wl["desc"], "grid": list(shape), "time_steps": T,
                    "bench_step": "one complete solve (all time steps) from resident initial fields",
                    "l2": "working set %.2f GB > 129 MB L2; no flush needed" % (16 * 4 * (nx + 1) * (ny + 1) * (nz + 1) / 1e9),
-                   "tiles": {"rows": by, "z_depth": kc, "cells_per_thread": vec},
+                   "tiles": {"rows": by, "z_depth": kc, "cells_per_thread": vec, "staged_planes": stages,
+                             "kernel": "k_yee_step_bulk" if stages else "k_yee_step"},
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src,

@@ -27,7 +27,7 @@ class FdtdParams(C.Structure):
 
 
 class TileConfig(C.Structure):
-    _fields_ = [("by", C.c_int), ("kc", C.c_int), ("vec", C.c_int)]
+    _fields_ = [("by", C.c_int), ("kc", C.c_int), ("vec", C.c_int), ("stages", C.c_int)]
 
 
 class ProblemDesc(C.Structure):

@@ -217,26 +217,9 @@ int rebuild_worklist(ptk_server *s)
     int rc = grow_worklist(s, n);
     if (rc) return rc;
     cudaStreamSynchronize(s->st);   // the pinned staging may still feed a previous copy
-    // x cells per thread for this launch: the widest tile whose share of lanes holding cells
-    // (weighted by the remaining work) is within 10 % of the best width's.
-    double eff[3] = {0, 0, 0}, work = 0;
-    const int vecs[3] = {1, 2, 4};
-    for (Inst *in : s->active) {
-        const double w = (double)in->L.nx * in->L.ny * in->L.nz * (in->steps_total - in->done);
-        work += w;
-        for (int v = 0; v < 3; ++v) {
-            const int tx = 32 * vecs[v];
-            eff[v] += w * in->L.nx / (double)(tx * ((in->L.nx + tx - 1) / tx));
-        }
-    }
-    const double best = std::max(eff[0], std::max(eff[1], eff[2]));
-    s->vec = 1;
-    for (int v = 2; v >= 0; --v)
-        if (eff[v] >= 0.9 * best) {
-            s->vec = vecs[v];
-            break;
-        }
-    (void)work;
+    // 128-wide tiles (4 cells per thread): narrower tiles keep more lanes busy on small grids but
+    // hold fewer bytes in flight per thread, and measured slower on the batched workload.
+    s->vec = 4;
     int tiles = 0;
     for (int q = 0; q < n; ++q) {
         Inst *in = s->active[q];

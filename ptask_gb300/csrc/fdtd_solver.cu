@@ -59,10 +59,10 @@ static void default_tiles(int nx, int ny, int nz, int *by, int *kc, int *vec)
 }
 
 struct GraphKey {
-    int len, by, kc, vec;
+    int len, by, kc, vec, stages;
     bool operator<(const GraphKey &o) const
     {
-        return std::tie(len, by, kc, vec) < std::tie(o.len, o.by, o.kc, o.vec);
+        return std::tie(len, by, kc, vec, stages) < std::tie(o.len, o.by, o.kc, o.vec, o.stages);
     }
 };
 
@@ -79,7 +79,8 @@ struct ptk_solver {
     int nwave = 0;
     long long src = -1;
     int step = 0;              // host mirror of the device step counter
-    int by = 0, kc = 0, vec = 4;
+    int by = 0, kc = 0, vec = 4, stages = 0;
+    int *d_err = nullptr;      // raised by the staged kernel if a bounded wait expires
     int total_tiles = 0;
     InstDesc *d_desc = nullptr;
     int *d_tile0 = nullptr;
@@ -130,7 +131,7 @@ static void drop_graphs(ptk_solver *s)
 // Graph of `len` fused steps + one advance for this solver's current tile shape.
 static int solver_graph(ptk_solver *s, int len, cudaGraphExec_t *out)
 {
-    GraphKey key{len, s->by, s->kc, s->vec};
+    GraphKey key{len, s->by, s->kc, s->vec, s->stages};
     auto it = s->graphs.find(key);
     if (it != s->graphs.end()) {
         *out = it->second;
@@ -141,7 +142,10 @@ static int solver_graph(ptk_solver *s, int len, cudaGraphExec_t *out)
     set_capturing(true);
     int rc = PTK_OK;
     for (int q = 0; q < len && rc == PTK_OK; ++q)
-        rc = launch_yee_step_v(s->d_desc, s->d_tile0, 1, s->total_tiles, q, s->by, s->vec, 0, s->cap);
+        rc = s->stages > 0
+                 ? launch_yee_step_bulk(s->d_desc, s->d_tile0, 1, s->total_tiles, q, s->by, s->stages, 0, s->d_err,
+                                        s->cap)
+                 : launch_yee_step_v(s->d_desc, s->d_tile0, 1, s->total_tiles, q, s->by, s->vec, 0, s->cap);
     if (rc == PTK_OK) rc = launch_advance(s->d_desc, 1, len, s->cap);
     set_capturing(false);
     cudaGraph_t g = nullptr;
@@ -225,6 +229,8 @@ int ptk_solver_create(const ptk_fdtd_params *p, ptk_solver **out)
     for (int c = 0; c < 4 && rc == PTK_OK; ++c) rc = pool_alloc(bytes, st, (void **)&s->coef[c]);
     if (rc == PTK_OK) rc = pool_alloc(sizeof(InstDesc), st, (void **)&s->d_desc);
     if (rc == PTK_OK) rc = pool_alloc(2 * sizeof(int), st, (void **)&s->d_tile0);
+    if (rc == PTK_OK) rc = pool_alloc(sizeof(int), st, (void **)&s->d_err);
+    if (rc == PTK_OK) cudaMemsetAsync(s->d_err, 0, sizeof(int), st);
     if (rc) {
         ptk_solver_destroy(s);
         return rc;
@@ -258,6 +264,7 @@ int ptk_solver_destroy(ptk_solver *s)
         pool_free(s->wave, st);
         pool_free(s->d_desc, st);
         pool_free(s->d_tile0, st);
+        pool_free(s->d_err, st);
         if (s->cap) cudaStreamDestroy(s->cap);
     }
     cudaStreamSynchronize(st);
@@ -315,7 +322,13 @@ int ptk_solver_get_fields(ptk_solver *s, float *const f[6], int where, void *str
             pool_free(stage, st);
         }
     }
-    if (where == PTK_HOST) PTK_CUDA_TRY(cudaStreamSynchronize(st));
+    if (where == PTK_HOST) {
+        PTK_CUDA_TRY(cudaStreamSynchronize(st));
+        int err = 0;
+        PTK_CUDA_TRY(cudaMemcpy(&err, s->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+        if (err)
+            return set_error(PTK_ERR_TIMEOUT, "a bounded wait of the staged step kernel expired; the fields are invalid");
+    }
     return PTK_OK;
 }
 
@@ -410,14 +423,19 @@ int ptk_solver_set_tiles(ptk_solver *s, const ptk_tile_config *cfg)
         default_tiles(s->p.Nx, s->p.Ny, s->p.Nz, &by, &kc, &dv);
         if (vec == 0) vec = dv;
     }
+    const int stages = cfg->stages;
+    if (stages > 0) vec = 4;
     if (vec == 0) vec = default_vec(s->p.Nx);
     PTK_CHECK_ARG(by == 4 || by == 8 || by == 16, "tile rows must be 4, 8 or 16 (got %d)", by);
     PTK_CHECK_ARG(vec == 1 || vec == 2 || vec == 4, "cells per thread must be 1, 2 or 4 (got %d)", vec);
+    PTK_CHECK_ARG(stages == 0 || yee_bulk_smem_bytes(by, stages) > 0,
+                  "no staged kernel for %d rows with %d stages", by, stages);
     PTK_CHECK_ARG(kc >= 0, "tile depth must be >= 0");
     if (kc >= s->p.Nz) kc = 0;
     s->by = by;
     s->kc = kc;
     s->vec = vec;
+    s->stages = stages;
     return PTK_OK;
 }
 
@@ -427,6 +445,7 @@ int ptk_solver_get_tiles(const ptk_solver *s, ptk_tile_config *cfg)
     cfg->by = s->by;
     cfg->kc = s->kc;
     cfg->vec = s->vec;
+    cfg->stages = s->stages;
     return PTK_OK;
 }
 
@@ -550,14 +569,23 @@ int ptk_autotune_tiles(int Nx, int Ny, int Nz, ptk_tile_config *best, float *bes
     const long long cells = (long long)Nx * Ny * Nz;
     const int steps = (int)std::max(4LL, std::min(64LL, 400000000LL / std::max(1LL, cells)));
     float best_t = 1e30f;
-    ptk_tile_config bc{8, 0, default_vec(Nx)};
-    const int vecs[3] = {1, 2, 4};
-    for (int vi = 0; vi < 3 * 3 * 6 && !rc; ++vi) {
-        const int vec = vecs[vi / 18], by = rows[(vi / 6) % 3], kc = depths[vi % 6];
+    ptk_tile_config bc{8, 0, default_vec(Nx), 0};
+    std::vector<ptk_tile_config> cands;
+    for (int vec : {1, 2, 4})
+        for (int by : rows)
+            for (int kc : depths) {
+                if (kc != 0 && kc >= Nz) continue;
+                if (32 * vec > 2 * std::max(Nx, 32)) continue;   // tiles far wider than the grid
+                cands.push_back({by, kc, vec, 0});
+            }
+    const int staged[7][2] = {{4, 2}, {4, 3}, {4, 4}, {8, 2}, {8, 3}, {8, 4}, {16, 2}};
+    for (const auto &bs : staged)
+        for (int kc : depths) {
+            if (kc == 8 || (kc != 0 && kc >= Nz)) continue;
+            cands.push_back({bs[0], kc, 4, bs[1]});
+        }
+    for (const ptk_tile_config &c : cands) {
         {
-            if (kc != 0 && kc >= Nz) continue;
-            if (32 * vec > 2 * std::max(Nx, 32)) continue;   // tiles far wider than the grid
-            ptk_tile_config c{by, kc, vec};
             if (ptk_solver_set_tiles(s, &c)) continue;
             if (ptk_solver_run(s, 2, st)) { rc = PTK_ERR_CUDA; break; }
             cudaEventRecord(e0, st);

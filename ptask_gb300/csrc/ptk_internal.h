@@ -91,6 +91,11 @@ int launch_yee_step_grid(const InstDesc *d_insts, const int *d_tile0, int ninst,
 // Same, for tiles planned with `vec` x cells per thread.
 int launch_yee_step_v(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles, int s_offset,
                       int by, int vec, int grid, cudaStream_t s);
+// The staged variant (operands brought into shared memory by bulk asynchronous copies, `stages`
+// planes in a ring; 128-wide tiles, vec == 4).  *err is raised if a bounded wait expires.
+int launch_yee_step_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles, int s_offset,
+                         int by, int stages, int grid, int *err, cudaStream_t s);
+size_t yee_bulk_smem_bytes(int by, int stages);
 // CTAs of the step kernel with `by` rows (and `vec`) that fit on the whole GPU at once.
 int yee_resident_ctas(int by);
 int yee_resident_ctas(int by, int vec);

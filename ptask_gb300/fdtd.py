@@ -150,15 +150,16 @@ class Solver:
     def set_vacuum(self, stream=None) -> None:
         call("ptk_solver_set_vacuum", self._h, stream)
 
-    def set_tiles(self, by: int, kc: int, vec: int = 0) -> None:
+    def set_tiles(self, by: int, kc: int, vec: int = 0, stages: int = 0) -> None:
         """Fused-kernel tile shape: `by` rows, `kc` z-planes (0 = all), `vec` x cells per thread
-        (1, 2, 4; 0 = chosen from Nx)."""
-        call("ptk_solver_set_tiles", self._h, C.byref(TileConfig(by, kc, vec)))
+        (1, 2, 4; 0 = chosen from Nx), `stages` > 0 selects the kernel whose operands are staged in
+        shared memory by bulk asynchronous copies (that many planes in the ring)."""
+        call("ptk_solver_set_tiles", self._h, C.byref(TileConfig(by, kc, vec, stages)))
 
-    def tiles(self) -> tuple[int, int, int]:
+    def tiles(self) -> tuple[int, int, int, int]:
         t = TileConfig()
         call("ptk_solver_get_tiles", self._h, C.byref(t))
-        return t.by, t.kc, t.vec
+        return t.by, t.kc, t.vec, t.stages
 
     def reset_clock(self) -> None:
         call("ptk_solver_reset_clock", self._h, None)
@@ -217,4 +218,4 @@ def tuned_tiles(nx: int, ny: int, nz: int) -> tuple[int, int, int]:
     t = TileConfig()
     ms = C.c_float()
     call("ptk_autotune_tiles", nx, ny, nz, C.byref(t), C.byref(ms))
-    return t.by, t.kc, t.vec
+    return t.by, t.kc, t.vec, t.stages

@@ -863,7 +863,7 @@ bool Graph::try_lower_cycle(Task *top)
                 plan->solver_params = *P;
                 plan->coef_key.clear();
                 if (rc == PTK_OK) {
-                    ptk_tile_config best{0, 0, 0};
+                    ptk_tile_config best{0, 0, 0, 0};
                     float ms = 0;
                     if (ptk_autotune_tiles(P->Nx, P->Ny, P->Nz, &best, &ms) == PTK_OK)
                         ptk_solver_set_tiles(plan->solver, &best);

@@ -246,3 +246,55 @@ def test_full_size_source_linearity(full_problem):
     b = P.solve(pr2, f, steps)
     for x, y in zip(a, b):
         assert oracle.normwise_error(y, x * np.float32(2)) <= 1e-6
+
+
+# ------------------------------------------------------------------------------------------------
+# The staged kernel (operands brought into shared memory by bulk asynchronous copies).
+# ------------------------------------------------------------------------------------------------
+STAGED = [(4, 2), (4, 3), (4, 4), (8, 2), (8, 3), (8, 4), (16, 2)]
+
+
+@pytest.mark.parametrize("by,stages", STAGED)
+@pytest.mark.parametrize("kc", [0, 1, 5])
+def test_staged_kernel_bitwise(by, stages, kc):
+    shape, steps = (261, 37, 23), 6      # x tiles 128+128+5: both halo ends clipped
+    pr = P.Problem.generate(*shape, n_boxes=3, eps=(1, 10), box=(5, 30), steps=steps, seed=14)
+    f = P.random_fields(*shape, seed=71, scale=1e-2)
+    ref = oracle.step_ext_f32(f, steps, pr.params, pr.Ca, pr.Cb, pr.Da, pr.Db, pr.src, pr.wave)
+    with P.Solver(pr.params) as s:
+        s.set_tiles(by, kc, 4, stages)
+        s.set_fields(f)
+        s.set_problem(pr)
+        s.run(steps)
+        assert_parity(s.get_fields(), ref, f"staged by={by} stages={stages} kc={kc}")
+
+
+@pytest.mark.parametrize("shape", [(5, 7, 3), (1, 1, 1), (2, 3, 2), (128, 9, 4), (129, 17, 6), (33, 64, 40)])
+def test_staged_kernel_small_and_edge_shapes(shape):
+    steps = 5
+    p = P.reference_params(*shape)
+    f = P.random_fields(*shape, seed=72)
+    ref = oracle.step_ref_f32(f, steps, p)
+    for by, stages in ((8, 3), (4, 2)):
+        with P.Solver(p) as s:
+            s.set_tiles(by, 3, 4, stages)
+            s.set_fields(f)
+            s.set_vacuum()
+            s.run(steps)
+            assert_parity(s.get_fields(), ref, f"staged {shape} by={by} stages={stages}")
+
+
+def test_staged_full_size_matches_register_kernel(full_problem):
+    pr = full_problem
+    f = P.zero_fields(*FULL)
+    outs = []
+    for tiles in ((4, 8, 4, 0), (8, 32, 4, 3), (4, 0, 4, 4)):
+        with P.Solver(pr.params) as s:
+            s.set_tiles(*tiles)
+            s.set_fields(f)
+            s.set_problem(pr)
+            s.run(300)
+            outs.append(s.get_fields())
+    for o in outs[1:]:
+        for a, b in zip(outs[0], o):
+            np.testing.assert_array_equal(a, b)
