@@ -578,7 +578,7 @@ int ptk_autotune_tiles(int Nx, int Ny, int Nz, ptk_tile_config *best, float *bes
                 if (32 * vec > 2 * std::max(Nx, 32)) continue;   // tiles far wider than the grid
                 cands.push_back({by, kc, vec, 0});
             }
-    const int staged[7][2] = {{4, 2}, {4, 3}, {4, 4}, {8, 2}, {8, 3}, {8, 4}, {16, 2}};
+    const int staged[5][2] = {{4, 3}, {4, 4}, {4, 5}, {8, 3}, {8, 4}};
     for (const auto &bs : staged)
         for (int kc : depths) {
             if (kc == 8 || (kc != 0 && kc >= Nz)) continue;

@@ -387,6 +387,9 @@ static int launch_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, i
     return PTK_OK;
 }
 
+// Rings of at least 3 stages: plane q waits for the stage of plane q+1 before its barrier, and a
+// stage is refilled only after the barrier of the plane that follows its last reader, so the stage
+// of plane q+1 must have been issued no later than plane q-1 (q+1-S+1 <= q-1).
 int launch_yee_step_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles, int s_offset,
                          int by, int stages, int grid, int *err, cudaStream_t s)
 {
@@ -394,9 +397,8 @@ int launch_yee_step_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst,
 #define PTK_BULK(B, S)                                                                                  \
     if (by == B && stages == S)                                                                         \
         return launch_bulk<B, S>(d_insts, d_tile0, ninst, total_tiles, s_offset, grid, err, s);
-    PTK_BULK(4, 2) PTK_BULK(4, 3) PTK_BULK(4, 4)
-    PTK_BULK(8, 2) PTK_BULK(8, 3) PTK_BULK(8, 4)
-    PTK_BULK(16, 2)
+    PTK_BULK(4, 3) PTK_BULK(4, 4) PTK_BULK(4, 5)
+    PTK_BULK(8, 3) PTK_BULK(8, 4)
 #undef PTK_BULK
     return set_error(PTK_ERR_INVALID, "no staged kernel for %d rows x %d stages", by, stages);
 }
@@ -405,9 +407,8 @@ size_t yee_bulk_smem_bytes(int by, int stages)
 {
 #define PTK_SM(B, S) \
     if (by == B && stages == S) return smem_bytes<B, S>();
-    PTK_SM(4, 2) PTK_SM(4, 3) PTK_SM(4, 4)
-    PTK_SM(8, 2) PTK_SM(8, 3) PTK_SM(8, 4)
-    PTK_SM(16, 2)
+    PTK_SM(4, 3) PTK_SM(4, 4) PTK_SM(4, 5)
+    PTK_SM(8, 3) PTK_SM(8, 4)
 #undef PTK_SM
     return 0;
 }

@@ -191,6 +191,10 @@ def test_bad_source_rejected():
             _lib.call("ptk_solver_set_source", s.handle, 0, 3, 3, w.ctypes.data, 4, 0, None)
         with pytest.raises(_lib.PtkError):
             s.set_tiles(5, 0)
+        with pytest.raises(_lib.PtkError):
+            s.set_tiles(8, 0, 4, 2)      # a two-stage ring cannot make progress: rejected
+        with pytest.raises(_lib.PtkError):
+            s.set_tiles(16, 0, 4, 3)     # three 16-row stages exceed shared memory: no such kernel
 
 
 # ------------------------------------------------------------------------------------------------
@@ -251,7 +255,7 @@ def test_full_size_source_linearity(full_problem):
 # ------------------------------------------------------------------------------------------------
 # The staged kernel (operands brought into shared memory by bulk asynchronous copies).
 # ------------------------------------------------------------------------------------------------
-STAGED = [(4, 2), (4, 3), (4, 4), (8, 2), (8, 3), (8, 4), (16, 2)]
+STAGED = [(4, 3), (4, 4), (4, 5), (8, 3), (8, 4)]
 
 
 @pytest.mark.parametrize("by,stages", STAGED)
@@ -275,7 +279,7 @@ def test_staged_kernel_small_and_edge_shapes(shape):
     p = P.reference_params(*shape)
     f = P.random_fields(*shape, seed=72)
     ref = oracle.step_ref_f32(f, steps, p)
-    for by, stages in ((8, 3), (4, 2)):
+    for by, stages in ((8, 3), (4, 5)):
         with P.Solver(p) as s:
             s.set_tiles(by, 3, 4, stages)
             s.set_fields(f)
