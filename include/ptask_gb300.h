@@ -162,9 +162,9 @@ typedef struct ptk_solver ptk_solver;
 
 /* Tile shape of the fused step kernel.  by: rows per CTA (4, 8 or 16); kc: z-planes per CTA (>=1,
  * 0 = whole depth); vec: x cells per thread (1, 2 or 4; tiles are 32*vec cells wide, 0 = choose
- * from Nx); stages: 0 = operands loaded into registers, 3..5 = operands staged into shared memory
- * by bulk asynchronous copies with that many z-planes in the ring (needs vec 4 and by 4 or 8; by 8
- * up to 4 stages).
+ * from Nx); stages: 0 = operands loaded into registers, 2..5 = operands staged into shared memory
+ * by TMA tensor copies with that many z-planes in the ring (needs vec 4 and by 4 or 8; by 8 up to
+ * 4 stages).
  * by = kc = 0 selects the default shape. */
 typedef struct ptk_tile_config {
     int by;

@@ -320,6 +320,28 @@ void plan_tiles(InstDesc &d, int by, int kc, int vec)
 
 void plan_tiles(InstDesc &d, int by, int kc) { plan_tiles(d, by, kc, 4); }
 
+int balanced_depths(int nx, int ny, int nz, int by, int vec, int resident, int *out, int n)
+{
+    if (resident <= 0 || n <= 0 || by <= 0 || vec <= 0) return 0;
+    const long long cols = (long long)((nx + 32 * vec - 1) / (32 * vec)) * ((ny + by - 1) / by);
+    std::vector<std::pair<long long, int>> c;
+    for (int tz = 1; tz <= nz; ++tz) {
+        const int kc = (nz + tz - 1) / tz;
+        if ((nz + kc - 1) / kc != tz) continue;   // same depth as a smaller tz
+        if (kc < 4) break;
+        const long long waves = (cols * tz + resident - 1) / resident;
+        c.push_back({waves * (kc + (tz > 1 ? 1 : 0) + 2), kc >= nz ? 0 : kc});
+    }
+    std::stable_sort(c.begin(), c.end(),
+                     [](const std::pair<long long, int> &a, const std::pair<long long, int> &b) { return a.first < b.first; });
+    int k = 0;
+    for (const auto &e : c) {
+        if (k == n) break;
+        out[k++] = e.second;
+    }
+    return k;
+}
+
 template <int BY, int V>
 static void launch_by_v(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles, int s_offset,
                         int g, cudaStream_t s)

@@ -81,6 +81,8 @@ struct ptk_solver {
     int step = 0;              // host mirror of the device step counter
     int by = 0, kc = 0, vec = 4, stages = 0;
     int *d_err = nullptr;      // raised by the staged kernel if a bounded wait expires
+    void *d_tma = nullptr;     // tensor maps of the staged kernel (encoded for tma_by rows)
+    int tma_by = 0;
     int total_tiles = 0;
     InstDesc *d_desc = nullptr;
     int *d_tile0 = nullptr;
@@ -114,6 +116,18 @@ static int solver_sync_desc(ptk_solver *s, int steps_left, cudaStream_t st)
 {
     InstDesc d = host_desc(s, steps_left);
     s->total_tiles = d.tiles_x * d.tiles_y * d.tiles_z + d.face_tiles;
+    if (s->stages > 0) {
+        if (s->tma_by != s->by) {
+            // The arrays never move, so the maps change only with the tile rows.
+            alignas(64) unsigned char maps[kTmaSetBytes];
+            int rc = encode_tma_set(d, s->by, maps);
+            if (rc) return rc;
+            PTK_CUDA_TRY(cudaStreamSynchronize(st));
+            PTK_CUDA_TRY(cudaMemcpy(s->d_tma, maps, kTmaSetBytes, cudaMemcpyHostToDevice));
+            s->tma_by = s->by;
+        }
+        d.tma = s->d_tma;
+    }
     int rc = store_desc(s->d_desc, d, st);
     if (rc) return rc;
     k_store_tile0<<<1, 1, 0, st>>>(s->d_tile0, 0, s->total_tiles);
@@ -230,6 +244,9 @@ int ptk_solver_create(const ptk_fdtd_params *p, ptk_solver **out)
     if (rc == PTK_OK) rc = pool_alloc(sizeof(InstDesc), st, (void **)&s->d_desc);
     if (rc == PTK_OK) rc = pool_alloc(2 * sizeof(int), st, (void **)&s->d_tile0);
     if (rc == PTK_OK) rc = pool_alloc(sizeof(int), st, (void **)&s->d_err);
+    if (rc == PTK_OK) rc = pool_alloc(kTmaSetBytes, st, &s->d_tma);
+    if (rc == PTK_OK && ((uintptr_t)s->d_tma & 63))
+        rc = set_error(PTK_ERR_CUDA, "tensor-map buffer is not 64-byte aligned");
     if (rc == PTK_OK) cudaMemsetAsync(s->d_err, 0, sizeof(int), st);
     if (rc) {
         ptk_solver_destroy(s);
@@ -265,6 +282,7 @@ int ptk_solver_destroy(ptk_solver *s)
         pool_free(s->d_desc, st);
         pool_free(s->d_tile0, st);
         pool_free(s->d_err, st);
+        pool_free(s->d_tma, st);
         if (s->cap) cudaStreamDestroy(s->cap);
     }
     cudaStreamSynchronize(st);
@@ -571,19 +589,25 @@ int ptk_autotune_tiles(int Nx, int Ny, int Nz, ptk_tile_config *best, float *bes
     float best_t = 1e30f;
     ptk_tile_config bc{8, 0, default_vec(Nx), 0};
     std::vector<ptk_tile_config> cands;
+    // Fixed depths plus the two that fill whole waves of resident CTAs best for each kernel.
+    auto add = [&](int by, int vec, int stages, int resident) {
+        std::vector<int> ks;
+        for (int kc : depths)
+            if (!(stages > 0 && kc == 8)) ks.push_back(kc);
+        int bal[2];
+        const int nb = balanced_depths(Nx, Ny, Nz, by, vec, resident, bal, 2);
+        for (int q = 0; q < nb; ++q)
+            if (std::find(ks.begin(), ks.end(), bal[q]) == ks.end()) ks.push_back(bal[q]);
+        for (int kc : ks)
+            if (kc == 0 || kc < Nz) cands.push_back({by, kc, vec, stages});
+    };
     for (int vec : {1, 2, 4})
-        for (int by : rows)
-            for (int kc : depths) {
-                if (kc != 0 && kc >= Nz) continue;
-                if (32 * vec > 2 * std::max(Nx, 32)) continue;   // tiles far wider than the grid
-                cands.push_back({by, kc, vec, 0});
-            }
-    const int staged[5][2] = {{4, 3}, {4, 4}, {4, 5}, {8, 3}, {8, 4}};
-    for (const auto &bs : staged)
-        for (int kc : depths) {
-            if (kc == 8 || (kc != 0 && kc >= Nz)) continue;
-            cands.push_back({bs[0], kc, 4, bs[1]});
+        for (int by : rows) {
+            if (32 * vec > 2 * std::max(Nx, 32)) continue;   // tiles far wider than the grid
+            add(by, vec, 0, yee_resident_ctas(by, vec));
         }
+    const int staged[7][2] = {{4, 2}, {4, 3}, {4, 4}, {4, 5}, {8, 2}, {8, 3}, {8, 4}};
+    for (const auto &bs : staged) add(bs[0], 4, bs[1], yee_bulk_resident_ctas(bs[0], bs[1]));
     for (const ptk_tile_config &c : cands) {
         {
             if (ptk_solver_set_tiles(s, &c)) continue;

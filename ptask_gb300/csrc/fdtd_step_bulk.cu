@@ -1,19 +1,28 @@
 // fdtd_step_bulk.cu -- the fused Yee step with its operands staged by the TMA engine.
 //
 // Same arithmetic, tiles, work list and results as k_yee_step (fdtd_kernels.cu), different data
-// movement.  For every z plane of a 128 x BY tile, the rows of all ten arrays that the plane needs
-// (own rows plus the y-1 / y+1 halo rows, 136 floats wide to cover the x-1 / x+1 halo with 16-byte
-// aligned copies) are fetched into shared memory by one-dimensional bulk asynchronous copies
-// (cp.async.bulk ... mbarrier::complete_tx::bytes).  Planes are loaded S-1 ahead into a ring of S
-// stages, each guarded by an mbarrier whose transaction count is the bytes in flight, so the number
-// of bytes in flight no longer depends on registers or occupancy: the SM keeps whole planes
-// streaming while its warps compute.  Compute reads only shared memory; results are written with
+// movement.  For every z plane of a 128 x BY tile, the rows of the ten arrays that the plane needs
+// (own rows plus the y-1 / y+1 halo rows, 136 floats wide to cover the x-1 / x+1 halo) arrive in
+// shared memory as one TMA tensor copy per array (cp.async.bulk.tensor.3d, box 136 x rows x 1):
+// ten copies per plane, issued by ten lanes of one warp.  Boxes that hang over the grid's edges are
+// filled with zeros by the TMA unit.  Planes are loaded ahead into a ring of S stages, each guarded
+// by an mbarrier whose transaction count is the bytes in flight, so the number of bytes in flight
+// does not depend on registers or occupancy.  Compute reads only shared memory; results leave with
 // 128-bit stores.  One block barrier per plane: new Hx, Hz rows are exchanged through a
 // double-buffered shared array, and a stage is refilled only after the barrier that follows its
 // last reader.
 //
-// Waits on an mbarrier are bounded; on expiry the kernel raises *err and stops using the stage
-// (results of that launch are then invalid and the host reports PTK_ERR_TIMEOUT).
+// Tensor maps (one per array and parity: 6 fields x 2 + 4 coefficients) are encoded on the host
+// (cuTensorMapEncodeTiled through the runtime's driver entry point) into device memory; the issuing
+// lane acquire-fences a map before its first use in a tile.
+//
+// Waits on an mbarrier are bounded; on expiry the kernel raises *err (results of that launch are
+// then invalid and the host reports PTK_ERR_TIMEOUT).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
 #include "fdtd_device.cuh"
 
 namespace ptk {
@@ -30,16 +39,28 @@ __host__ __device__ constexpr int row_lo(int a) { return (a == A_HY || a == A_CA
 template <int BY>
 __host__ __device__ constexpr int row_hi(int a) { return (a == A_EX || a == A_EZ) ? BY + 2 : BY + 1; }
 template <int BY>
-__host__ __device__ constexpr int row_off(int a)   // first row of array a inside a stage
+__host__ __device__ constexpr int rows_of(int a) { return row_hi<BY>(a) - row_lo(a); }
+// Each array's region in a stage starts on a 128-byte boundary (TMA destination alignment).
+template <int BY>
+__host__ __device__ constexpr int region_bytes(int a) { return (rows_of<BY>(a) * kRowW * 4 + 127) / 128 * 128; }
+template <int BY>
+__host__ __device__ constexpr int region_off(int a)
 {
     int o = 0;
-    for (int q = 0; q < a; ++q) o += row_hi<BY>(q) - row_lo(q);
+    for (int q = 0; q < a; ++q) o += region_bytes<BY>(q);
     return o;
 }
 template <int BY>
-__host__ __device__ constexpr int stage_rows() { return row_off<BY>(A_N); }
+__host__ __device__ constexpr size_t stage_bytes() { return (size_t)region_off<BY>(A_N); }
 template <int BY>
-__host__ __device__ constexpr size_t stage_bytes() { return (size_t)stage_rows<BY>() * kRowW * sizeof(float); }
+__host__ __device__ constexpr uint32_t box_bytes(int a) { return (uint32_t)(rows_of<BY>(a) * kRowW * 4); }
+template <int BY>
+__host__ __device__ constexpr uint32_t plane_tx_bytes()
+{
+    uint32_t t = 0;
+    for (int a = 0; a < A_N; ++a) t += box_bytes<BY>(a);
+    return t;
+}
 template <int BY>
 __host__ __device__ constexpr size_t xchg_bytes() { return (size_t)2 * 2 * (BY + 1) * 32 * sizeof(float4); }
 template <int BY, int S>
@@ -76,12 +97,18 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
     return false;
 }
 
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar)
 {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_acquire(const CUtensorMap *map)
+{
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(map) : "memory");
 }
 
 __device__ __forceinline__ float4 ld4s(const float *p) { return *reinterpret_cast<const float4 *>(p); }
@@ -93,50 +120,29 @@ __device__ __forceinline__ float yee_b(float d, float h, float c, float a1, floa
     return __fadd_rn(__fmul_rn(d, h), __fmul_rn(c, curl));
 }
 
-struct TileGeom {
-    const float *src[A_N];   // plane-0 base of each array (fields of the current parity)
-    long long plane;
-    int pitch, ny, x0, y0, xs, xe;   // staged x range [xs, xe) in global floats
-};
-
-// Issue the copies of plane k into stage buffer `st` (called by the 32 lanes of one warp).
-template <int BY>
-__device__ __forceinline__ void issue_plane(const TileGeom &g, int k, bool next_only, float *st, uint64_t *bar,
-                                            int lane)
+// Map of array a for field parity par in an instance's 16-map set.
+__device__ __forceinline__ const CUtensorMap *map_of(const CUtensorMap *set, int a, int par)
 {
-    const uint32_t row_bytes = (uint32_t)(g.xe - g.xs) * 4u;
-    const int dx = g.xs - (g.x0 - 4);   // destination offset inside a staged row (floats)
-    // count the rows first so that the transaction count is registered before any copy lands
-    uint32_t rows = 0;
-#pragma unroll
-    for (int a = 0; a < A_N; ++a) {
-        if (next_only && a != A_EX && a != A_EY) continue;
-        for (int r = row_lo(a); r < row_hi<BY>(a); ++r) {
-            const int j = g.y0 - 1 + r;
-            if (j >= 0 && j <= g.ny) ++rows;
-        }
-    }
-    if (lane == 0) mbar_expect_tx(bar, rows * row_bytes);
+    return a < 6 ? set + par * 6 + a : set + 12 + (a - 6);
+}
+
+// Issue plane k of the tile into stage buffer `st` (called by the 32 lanes of one warp; lanes
+// 0..9 each issue one array's box).
+template <int BY>
+__device__ __forceinline__ void issue_plane(const CUtensorMap *set, int par, int x0, int y0, int k, bool next_only,
+                                            unsigned char *st, uint64_t *bar, int lane)
+{
+    if (lane == 0)
+        mbar_expect_tx(bar, next_only ? box_bytes<BY>(A_EX) + box_bytes<BY>(A_EY) : plane_tx_bytes<BY>());
     __syncwarp();
-    int n = 0;
-#pragma unroll
-    for (int a = 0; a < A_N; ++a) {
-        if (next_only && a != A_EX && a != A_EY) continue;
-        for (int r = row_lo(a); r < row_hi<BY>(a); ++r) {
-            const int j = g.y0 - 1 + r;
-            if (j < 0 || j > g.ny) continue;
-            if ((n++ & 31) != lane) continue;
-            const float *src = g.src[a] + g.xs + (long long)g.pitch * j + g.plane * k;
-            float *dst = st + (size_t)(row_off<BY>(a) + r - row_lo(a)) * kRowW + dx;
-            bulk_g2s(dst, src, row_bytes, bar);
-        }
-    }
+    if (lane < A_N && (!next_only || lane == A_EX || lane == A_EY))
+        tma_load_3d(st + region_off<BY>(lane), map_of(set, lane, par), x0 - 4, y0 - 1 + row_lo(lane), k, bar);
 }
 
 template <int BY>
-__device__ __forceinline__ const float *row_ptr(const float *st, int a, int r)
+__device__ __forceinline__ const float *row_ptr(const unsigned char *st, int a, int r)
 {
-    return st + (size_t)(row_off<BY>(a) + r - row_lo(a)) * kRowW;
+    return reinterpret_cast<const float *>(st + region_off<BY>(a)) + (size_t)(r - row_lo(a)) * kRowW;
 }
 
 }  // namespace
@@ -147,11 +153,15 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
                 int total_tiles, int *err)
 {
     extern __shared__ __align__(128) unsigned char smem[];
-    float *stages = reinterpret_cast<float *>(smem);
+    unsigned char *stages = smem;
     float4 *xchg = reinterpret_cast<float4 *>(smem + S * stage_bytes<BY>());   // [2 buf][2 arr][BY+1][32]
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + S * stage_bytes<BY>() + xchg_bytes<BY>());
 
     const int lane = threadIdx.x, ty = threadIdx.y;
+    if (smem_u32(smem) & 127u) {   // TMA destinations need 128-byte alignment: refuse, do not fault
+        if (ty == 0 && lane == 0) atomicOr(err, 2);
+        return;
+    }
     if (ty == 0 && lane == 0) {
         for (int s = 0; s < S; ++s) mbar_init(&bars[s], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -181,6 +191,7 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
         const int nx = D->nx, ny = D->ny, nz = D->nz, pitch = D->pitch, kc = D->kc;
         const long long plane = D->plane;
         const float cx = D->cx, cy = D->cy, cz = D->cz;
+        const CUtensorMap *maps = reinterpret_cast<const CUtensorMap *>(D->tma);
         float *__restrict__ oHx = D->buf[par ^ 1][0];
         float *__restrict__ oHy = D->buf[par ^ 1][1];
         float *__restrict__ oHz = D->buf[par ^ 1][2];
@@ -194,26 +205,17 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
         const int xt = r0 % D->tiles_x; r0 /= D->tiles_x;
         const int yt = r0 % D->tiles_y;
         const int zt = r0 / D->tiles_y;
-        TileGeom g;
-        for (int f = 0; f < 6; ++f) g.src[f] = D->buf[par][f];
-        for (int c = 0; c < 4; ++c) g.src[6 + c] = D->coef[c];
-        g.plane = plane;
-        g.pitch = pitch;
-        g.ny = ny;
-        g.x0 = xt * 128;
-        g.y0 = yt * BY;
-        g.xs = max(g.x0 - 4, 0);
-        g.xe = min(g.x0 + 132, pitch);
-        const int x0 = g.x0, y0 = g.y0;
+        const int x0 = xt * 128, y0 = yt * BY;
         const int k0 = zt * kc, k1 = min(k0 + kc, nz);
         const int kstart = k0 > 0 ? k0 - 1 : k0;
         const int nplanes = k1 - kstart + 1;   // planes kstart..k1 (k1 is read as "next" only)
 
         // prologue: the first S planes
         if (ty == 0) {
+            if (lane < A_N) tma_acquire(map_of(maps, lane, par));
             for (int q = 0; q < S && q < nplanes; ++q) {
                 const unsigned G = gbase + q;
-                issue_plane<BY>(g, kstart + q, kstart + q == k1, stages + (size_t)(G % S) * (stage_bytes<BY>() / 4),
+                issue_plane<BY>(maps, par, x0, y0, kstart + q, kstart + q == k1, stages + (size_t)(G % S) * stage_bytes<BY>(),
                                 &bars[G % S], lane);
             }
         }
@@ -234,8 +236,8 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
         for (int k = kstart; k < k1; ++k, off += plane) {
             const int q = k - kstart;
             const unsigned Gc = gbase + q, Gn = Gc + 1;
-            const float *cur = stages + (size_t)(Gc % S) * (stage_bytes<BY>() / 4);
-            const float *nxt = stages + (size_t)(Gn % S) * (stage_bytes<BY>() / 4);
+            const unsigned char *cur = stages + (size_t)(Gc % S) * stage_bytes<BY>();
+            const unsigned char *nxt = stages + (size_t)(Gn % S) * stage_bytes<BY>();
             if (!failed) {
                 bool ok = mbar_wait(&bars[Gc % S], (Gc / S) & 1);
                 ok = ok && mbar_wait(&bars[Gn % S], (Gn / S) & 1);
@@ -246,7 +248,7 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
             }
             const bool warm = (k < k0);
             float4 hx = make_float4(0, 0, 0, 0), hy = hx, hz = hx, ez = hx, ex0 = hx, ey0 = hx, ex1 = hx, ey1 = hx;
-            float4 exj1 = hx, ezj1 = hx, da = hx, db = hx;
+            float4 exj1 = hx, ezj1 = hx, da = hx, db = hx, ca = hx, cb = hx;
             float ez_l = 0.f, ey_l = 0.f;
             const bool act = xin && (halo ? (jrow && !warm) : jrow);
             if (act) {
@@ -263,6 +265,8 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
                 if (!halo) {
                     hy = ld4s(row_ptr<BY>(cur, A_HY, r) + xl);
                     ex1 = ld4s(row_ptr<BY>(nxt, A_EX, r) + xl);
+                    ca = ld4s(row_ptr<BY>(cur, A_CA, r) + xl);
+                    cb = ld4s(row_ptr<BY>(cur, A_CB, r) + xl);
                 }
                 if (lane == 31) {
                     ez_l = row_ptr<BY>(cur, A_EZ, r)[xl + 4];
@@ -304,11 +308,12 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
                 sH[(BY + 1) * 32 + ty * 32 + lane] = make_float4(hzn[0], hzn[1], hzn[2], hzn[3]);
             }
             __syncthreads();
-            // every reader of the stage of plane k-1 has passed the barrier: refill it
-            if (ty == 0 && q >= 1 && q - 1 + S < nplanes) {
-                const unsigned G = gbase + q - 1 + S;
-                issue_plane<BY>(g, kstart + q - 1 + S, kstart + q - 1 + S == k1,
-                                stages + (size_t)(G % S) * (stage_bytes<BY>() / 4), &bars[G % S], lane);
+            // Plane k's stage was read (as "next") before the previous barrier and (as "current")
+            // before this one, and nothing after this barrier reads a stage: refill it now.
+            if (ty == 0 && q + S < nplanes) {
+                const unsigned G = gbase + q + S;
+                issue_plane<BY>(maps, par, x0, y0, kstart + q + S, kstart + q + S == k1,
+                                stages + (size_t)(G % S) * stage_bytes<BY>(), &bars[G % S], lane);
             }
             float hy_p = __shfl_up_sync(0xffffffffu, hyn[3], 1);
             float hz_p = __shfl_up_sync(0xffffffffu, hzn[3], 1);
@@ -318,8 +323,7 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
                     const float4 hxj4 = sH[(ty - 1) * 32 + lane];
                     const float4 hzj4 = sH[(BY + 1) * 32 + (ty - 1) * 32 + lane];
                     const float hxj[4] = {hxj4.x, hxj4.y, hxj4.z, hxj4.w}, hzj[4] = {hzj4.x, hzj4.y, hzj4.z, hzj4.w};
-                    const float4 ca4 = ld4s(row_ptr<BY>(cur, A_CA, r) + xl), cb4 = ld4s(row_ptr<BY>(cur, A_CB, r) + xl);
-                    const float cav[4] = {ca4.x, ca4.y, ca4.z, ca4.w}, cbv[4] = {cb4.x, cb4.y, cb4.z, cb4.w};
+                    const float cav[4] = {ca.x, ca.y, ca.z, ca.w}, cbv[4] = {cb.x, cb.y, cb.z, cb.w};
                     const float hxpv[4] = {hxp.x, hxp.y, hxp.z, hxp.w}, hypv[4] = {hyp.x, hyp.y, hyp.z, hyp.w};
                     float exn[4], eyn[4], ezn[4];
 #pragma unroll
@@ -369,17 +373,37 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
         for (unsigned G = gbase > (unsigned)S ? gbase - S : 0u; G < gbase; ++G) mbar_wait(&bars[G % S], (G / S) & 1);
 }
 
+// Opt the instantiation into its dynamic shared memory (once per process; repeating it is harmless).
+template <int BY, int S>
+static int prepare_bulk()
+{
+    static bool attr_set = false;
+    if (!attr_set) {
+        PTK_CUDA_TRY(cudaFuncSetAttribute(k_yee_step_bulk<BY, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem_bytes<BY, S>()));
+        attr_set = true;
+    }
+    return PTK_OK;
+}
+
+template <int BY, int S>
+static int resident_bulk()
+{
+    if (prepare_bulk<BY, S>()) return 0;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_yee_step_bulk<BY, S>, 32 * (BY + 1),
+                                                      smem_bytes<BY, S>()) != cudaSuccess)
+        return 0;
+    return per_sm * std::max(1, sm_count());
+}
+
 template <int BY, int S>
 static int launch_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles, int s_offset,
                        int grid, int *err, cudaStream_t s)
 {
-    static bool attr_set = false;
     const size_t smem = smem_bytes<BY, S>();
-    if (!attr_set) {
-        PTK_CUDA_TRY(cudaFuncSetAttribute(k_yee_step_bulk<BY, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)smem));
-        attr_set = true;
-    }
+    int rc = prepare_bulk<BY, S>();
+    if (rc) return rc;
     const int g = (grid <= 0 || grid > total_tiles) ? total_tiles : grid;
     k_yee_step_bulk<BY, S><<<g, dim3(32, BY + 1), smem, s>>>(d_insts, d_tile0, ninst, s_offset, total_tiles, err);
     PTK_CUDA_TRY(cudaGetLastError());
@@ -387,9 +411,8 @@ static int launch_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, i
     return PTK_OK;
 }
 
-// Rings of at least 3 stages: plane q waits for the stage of plane q+1 before its barrier, and a
-// stage is refilled only after the barrier of the plane that follows its last reader, so the stage
-// of plane q+1 must have been issued no later than plane q-1 (q+1-S+1 <= q-1).
+// Rings of at least 2 stages: plane q waits for the stage of plane q+1 before its barrier, and the
+// stage of plane q+1 is issued after the barrier of plane q+1-S, so q+1-S <= q-1.
 int launch_yee_step_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles, int s_offset,
                          int by, int stages, int grid, int *err, cudaStream_t s)
 {
@@ -397,8 +420,8 @@ int launch_yee_step_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst,
 #define PTK_BULK(B, S)                                                                                  \
     if (by == B && stages == S)                                                                         \
         return launch_bulk<B, S>(d_insts, d_tile0, ninst, total_tiles, s_offset, grid, err, s);
-    PTK_BULK(4, 3) PTK_BULK(4, 4) PTK_BULK(4, 5)
-    PTK_BULK(8, 3) PTK_BULK(8, 4)
+    PTK_BULK(4, 2) PTK_BULK(4, 3) PTK_BULK(4, 4) PTK_BULK(4, 5)
+    PTK_BULK(8, 2) PTK_BULK(8, 3) PTK_BULK(8, 4)
 #undef PTK_BULK
     return set_error(PTK_ERR_INVALID, "no staged kernel for %d rows x %d stages", by, stages);
 }
@@ -407,10 +430,66 @@ size_t yee_bulk_smem_bytes(int by, int stages)
 {
 #define PTK_SM(B, S) \
     if (by == B && stages == S) return smem_bytes<B, S>();
-    PTK_SM(4, 3) PTK_SM(4, 4) PTK_SM(4, 5)
-    PTK_SM(8, 3) PTK_SM(8, 4)
+    PTK_SM(4, 2) PTK_SM(4, 3) PTK_SM(4, 4) PTK_SM(4, 5)
+    PTK_SM(8, 2) PTK_SM(8, 3) PTK_SM(8, 4)
 #undef PTK_SM
     return 0;
+}
+
+int yee_bulk_resident_ctas(int by, int stages)
+{
+#define PTK_RES(B, S) \
+    if (by == B && stages == S) return resident_bulk<B, S>();
+    PTK_RES(4, 2) PTK_RES(4, 3) PTK_RES(4, 4) PTK_RES(4, 5)
+    PTK_RES(8, 2) PTK_RES(8, 3) PTK_RES(8, 4)
+#undef PTK_RES
+    return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Tensor maps.
+// ---------------------------------------------------------------------------------------------
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
+{
+    static std::once_flag once;
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+template <int BY>
+static int encode_set(const InstDesc &d, CUtensorMap *out)
+{
+    PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+    if (!enc) return set_error(PTK_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    const cuuint64_t dims[3] = {(cuuint64_t)d.pitch, (cuuint64_t)d.ny + 1, (cuuint64_t)d.nz + 1};
+    const cuuint64_t strides[2] = {(cuuint64_t)d.pitch * 4, (cuuint64_t)d.plane * 4};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    for (int m = 0; m < 16; ++m) {
+        const int a = m < 12 ? m % 6 : 6 + (m - 12);
+        void *base = m < 12 ? (void *)d.buf[m / 6][m % 6] : (void *)d.coef[m - 12];
+        const cuuint32_t box[3] = {(cuuint32_t)kRowW, (cuuint32_t)rows_of<BY>(a), 1};
+        CUresult r = enc(&out[m], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return set_error(PTK_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d) for map %d", (int)r, m);
+    }
+    return PTK_OK;
+}
+
+int encode_tma_set(const InstDesc &d, int by, void *host_out)
+{
+    CUtensorMap *out = static_cast<CUtensorMap *>(host_out);
+    if (by == 4) return encode_set<4>(d, out);
+    if (by == 8) return encode_set<8>(d, out);
+    return set_error(PTK_ERR_INVALID, "no staged kernel for %d rows", by);
 }
 
 }  // namespace ptk

@@ -2,9 +2,12 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cstddef>
 #include <cstdint>
 #include <string>
+#include <utility>
+#include <vector>
 
 #include "../../include/ptask_gb300.h"
 
@@ -70,7 +73,14 @@ struct InstDesc {
     int tiles_x, tiles_y, tiles_z, face_tiles;
     int kc;                    // z-planes per main tile
     int vec;                   // x cells per thread: main tiles are 32*vec cells wide
+    const void *tma;           // staged kernel only: 16 tensor maps (6 fields x 2 parities, 4 coefs)
 };
+
+// Bytes of one instance's tensor-map set (16 CUtensorMap of 128 bytes; 64-byte alignment).
+constexpr size_t kTmaSetBytes = 16 * 128;
+// Encode the tensor maps of `d`'s arrays for the staged kernel with `by` tile rows into host
+// memory (kTmaSetBytes).
+int encode_tma_set(const InstDesc &d, int by, void *host_out);
 
 // Shape of the fused step kernel's main tiles (x width is fixed at 128 cells).
 constexpr int kTileX = 128;
@@ -91,11 +101,17 @@ int launch_yee_step_grid(const InstDesc *d_insts, const int *d_tile0, int ninst,
 // Same, for tiles planned with `vec` x cells per thread.
 int launch_yee_step_v(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles, int s_offset,
                       int by, int vec, int grid, cudaStream_t s);
-// The staged variant (operands brought into shared memory by bulk asynchronous copies, `stages`
-// planes in a ring; 128-wide tiles, vec == 4).  *err is raised if a bounded wait expires.
+// The staged variant (operands brought into shared memory by TMA tensor copies, `stages` planes
+// in a ring; 128-wide tiles, vec == 4; every instance's `tma` set encoded for `by`).  *err is
+// raised if a bounded wait expires.
 int launch_yee_step_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles, int s_offset,
                          int by, int stages, int grid, int *err, cudaStream_t s);
 size_t yee_bulk_smem_bytes(int by, int stages);
+// CTAs of the staged kernel that fit on the whole GPU at once (0: no such kernel).
+int yee_bulk_resident_ctas(int by, int stages);
+// Z depths (at most `n`, best first) whose tile count fills whole waves of `resident` CTAs with the
+// least work per CTA: each CTA's cost is its planes plus the warm plane and the pipeline fill.
+int balanced_depths(int nx, int ny, int nz, int by, int vec, int resident, int *out, int n);
 // CTAs of the step kernel with `by` rows (and `vec`) that fit on the whole GPU at once.
 int yee_resident_ctas(int by);
 int yee_resident_ctas(int by, int vec);

@@ -153,7 +153,7 @@ class Solver:
     def set_tiles(self, by: int, kc: int, vec: int = 0, stages: int = 0) -> None:
         """Fused-kernel tile shape: `by` rows, `kc` z-planes (0 = all), `vec` x cells per thread
         (1, 2, 4; 0 = chosen from Nx), `stages` > 0 selects the kernel whose operands are staged in
-        shared memory by bulk asynchronous copies (that many planes in the ring)."""
+        shared memory by TMA tensor copies (that many planes in the ring, 2..5)."""
         call("ptk_solver_set_tiles", self._h, C.byref(TileConfig(by, kc, vec, stages)))
 
     def tiles(self) -> tuple[int, int, int, int]:

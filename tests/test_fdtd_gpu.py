@@ -192,7 +192,7 @@ def test_bad_source_rejected():
         with pytest.raises(_lib.PtkError):
             s.set_tiles(5, 0)
         with pytest.raises(_lib.PtkError):
-            s.set_tiles(8, 0, 4, 2)      # a two-stage ring cannot make progress: rejected
+            s.set_tiles(8, 0, 4, 1)      # a one-stage ring cannot make progress: rejected
         with pytest.raises(_lib.PtkError):
             s.set_tiles(16, 0, 4, 3)     # three 16-row stages exceed shared memory: no such kernel
 
@@ -253,9 +253,9 @@ def test_full_size_source_linearity(full_problem):
 
 
 # ------------------------------------------------------------------------------------------------
-# The staged kernel (operands brought into shared memory by bulk asynchronous copies).
+# The staged kernel (operands brought into shared memory by TMA tensor copies).
 # ------------------------------------------------------------------------------------------------
-STAGED = [(4, 3), (4, 4), (4, 5), (8, 3), (8, 4)]
+STAGED = [(4, 2), (4, 3), (4, 4), (4, 5), (8, 2), (8, 3), (8, 4)]
 
 
 @pytest.mark.parametrize("by,stages", STAGED)
@@ -279,7 +279,7 @@ def test_staged_kernel_small_and_edge_shapes(shape):
     p = P.reference_params(*shape)
     f = P.random_fields(*shape, seed=72)
     ref = oracle.step_ref_f32(f, steps, p)
-    for by, stages in ((8, 3), (4, 5)):
+    for by, stages in ((8, 2), (4, 5)):
         with P.Solver(p) as s:
             s.set_tiles(by, 3, 4, stages)
             s.set_fields(f)
