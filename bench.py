@@ -153,9 +153,9 @@ def hbm_peak():
     return FALLBACK_HBM_GBS, "fallback"
 
 
-def traffic_per_cell():
-    """DRAM bytes per cell update of the fused step kernel from the committed ncu summary, if any."""
-    f = ROOT / "profiles" / "yee_step_256.md"
+def traffic_per_cell(kernel: str):
+    """DRAM bytes per cell update of the given fused step kernel from its committed ncu summary."""
+    f = ROOT / "profiles" / ("yee_step_bulk_256.md" if kernel == "k_yee_step_bulk" else "yee_step_256.md")
     if not f.exists():
         return None
     for line in f.read_text().splitlines():
@@ -320,8 +320,9 @@ def run_ours(args, wl, world, rank, local):
     per_launch_ms = statistics.median(run_ms) / T
     peak, peak_src = hbm_peak()
     achieved = BYTES_PER_CELL * cells / (per_launch_ms / 1e3) / 1e9
-    tpc = traffic_per_cell()
     by, kc, vec, stages = solver.tiles()
+    kernel = "k_yee_step_bulk" if stages else "k_yee_step"
+    tpc = traffic_per_cell(kernel)
     line = {
         "metric": "FDTD Mcell-updates/s", "value": value, "unit": "Mcell-updates/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
@@ -331,12 +332,12 @@ def run_ours(args, wl, world, rank, local):
                    "bench_step": "one complete solve (all time steps) from resident initial fields",
                    "l2": "working set %.2f GB > 129 MB L2; no flush needed" % (16 * 4 * (nx + 1) * (ny + 1) * (nz + 1) / 1e9),
                    "tiles": {"rows": by, "z_depth": kc, "cells_per_thread": vec, "staged_planes": stages,
-                             "kernel": "k_yee_step_bulk" if stages else "k_yee_step"},
+                             "kernel": kernel},
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src,
                      "traffic": (tpc * cells) if tpc else None,
-                     "kernel": "k_yee_step (fused H+E step)",
+                     "kernel": kernel + " (fused H+E step)",
                      "algorithmic_bytes_per_launch": BYTES_PER_CELL * cells,
                      "launch_ms": per_launch_ms},
         "e2e": {"value": e2e_value, "unit": "Mcell-updates/s", "h2d_bytes_per_step": h2d,
