@@ -359,7 +359,7 @@ def run_served(args, kind, world, rank, local):
     plain one-at-a-time dispatch of the same requests."""
     import ptask_gb300 as P
     from ptask_gb300 import _lib
-    from ptask_gb300.serve import Server, batched_instances, poisson_trace
+    from ptask_gb300.serve import Server, batched_instances, graph_dispatch, poisson_trace
 
     _lib.call("ptk_runtime_init", local)
     if kind == "batched":
@@ -393,6 +393,7 @@ def run_served(args, kind, world, rank, local):
     runs = [serve(0) for _ in range(args.steps)]
     clk = clocks.stop()
     plain = serve(1)
+    pgraph = None if args.no_plain_graph else graph_dispatch(reqs, scale, mode="taskwise")
     best = min(runs, key=lambda s: s["wall_s"])
     wall = statistics.median(s["wall_s"] for s in runs)
     value = len(reqs) / wall
@@ -409,6 +410,14 @@ def run_served(args, kind, world, rank, local):
                   "p50_latency_s": plain["p50_latency_s"], "p99_latency_s": plain["p99_latency_s"],
                   "wall_s": plain["wall_s"]},
         "speedup_vs_plain": (len(reqs) / wall) / (len(reqs) / plain["wall_s"]),
+        "plain_graph": None if pgraph is None else {
+            "dispatch": "one PTask FDTD graph per request shape, one request at a time, H and E tasks "
+                        "dispatched per iteration by the scheduler; inputs pushed, six fields pulled",
+            "solves_per_s": pgraph["solves"] / pgraph["wall_s"],
+            "mcell_updates_per_s": cells / pgraph["wall_s"] / 1e6,
+            "p50_latency_s": pgraph["p50_latency_s"], "p99_latency_s": pgraph["p99_latency_s"],
+            "wall_s": pgraph["wall_s"]},
+        "speedup_vs_plain_graph": None if pgraph is None else (len(reqs) / wall) / (pgraph["solves"] / pgraph["wall_s"]),
         "gpu_launches": int(best["launches"]),
         "clocks": clk,
     }
@@ -428,6 +437,8 @@ def main() -> int:
     ap.add_argument("--tiles", default=None, help="fixed tile shape ROWS,DEPTH (skips the autotuner)")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain-graph", action="store_true",
+                    help="batched/served: skip the per-graph (task-wise) plain dispatch arm")
     args = ap.parse_args()
     world, rank, local = dist_env()
     if args.workload in ("batched", "served") and args.impl == "ours":

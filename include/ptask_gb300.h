@@ -243,6 +243,8 @@ typedef struct ptk_server_config {
     int tile_rows;             /* fused-kernel tile rows 4, 8 or 16 (0: 8) */
     int keep_results;          /* keep finished fields for ptk_server_fetch */
     int persistent;            /* persistent grid of resident CTAs instead of one CTA per tile */
+    int stages;                /* step kernel: 0 = TMA-staged with its default ring (tile_rows 4 or 8,
+                                  else 8), 2..5 = TMA-staged with that many planes, -1 = register kernel */
 } ptk_server_config;
 
 typedef struct ptk_request_info {

@@ -39,7 +39,7 @@ class ProblemDesc(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_active", C.c_int), ("chunk_steps", C.c_int),
-                ("tile_rows", C.c_int), ("keep_results", C.c_int), ("persistent", C.c_int)]
+                ("tile_rows", C.c_int), ("keep_results", C.c_int), ("persistent", C.c_int), ("stages", C.c_int)]
 
 
 class RequestInfo(C.Structure):

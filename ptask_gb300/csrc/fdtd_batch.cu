@@ -76,6 +76,7 @@ struct Inst {
     float *buf[2][6] = {};
     float *coef[4] = {};
     float *wave = nullptr;
+    void *tma = nullptr;        // tensor maps of the staged kernel
     int nwave = 0;
     long long src = -1;
     int steps_total = 0, done = 0;
@@ -90,7 +91,8 @@ struct Inst {
 
 size_t instance_bytes(const Layout &L, int nwave)
 {
-    return (size_t)L.total * sizeof(float) * 16 + (size_t)nwave * sizeof(float) + 6 * sizeof(double) + 4096;
+    return (size_t)L.total * sizeof(float) * 16 + (size_t)nwave * sizeof(float) + 6 * sizeof(double) + kTmaSetBytes +
+           4096;
 }
 
 }  // namespace ptk
@@ -113,6 +115,12 @@ struct ptk_server {
     int cap = 0;
     int total_tiles = 0;
     int vec = 4;                    // x cells per thread of the current work list
+    int rows = 8, stages = 4;       // step kernel: tile rows; staged ring planes (0 = register kernel)
+    int *d_err = nullptr;           // raised by the staged kernel if a bounded wait expires
+    int *d_work = nullptr;          // staged kernel's tile counters, one per step of a chunk
+    int depth_cap = 0;              // staged kernel: deepest z chunk of the current work list
+    int resident = 1;               // CTAs of the step kernel that fit on the GPU at once
+    int *h_err = nullptr;           // pinned copy, read after every chunk
     bool dirty = true;
     std::map<std::tuple<int, int, int, int>, cudaGraphExec_t> graphs;
     long long chunks = 0, launches = 0;
@@ -150,6 +158,60 @@ int grow_worklist(ptk_server *s, int n)
     return PTK_OK;
 }
 
+// Tile depth (0 = whole) of an instance nz planes deep under a cap: near-equal chunks of at most
+// `cap` planes.  The register kernel keeps the short chunks it was tuned with.
+int depth_for_cap(int nz, int cap)
+{
+    if (nz <= cap) return 0;
+    const int parts = (nz + cap - 1) / cap;
+    return (nz + parts - 1) / parts;
+}
+
+int instance_depth(const ptk_server *s, int nz)
+{
+    if (!s->stages) return nz > 48 ? 16 : 0;
+    return depth_for_cap(nz, s->depth_cap);
+}
+
+// Deepest cap (planes per staged tile) that still gives the work list a few tiles per resident CTA:
+// deep tiles pay the pipeline fill and the warm plane rarely, but one small instance alone needs
+// shallow tiles to occupy the GPU.
+int choose_depth_cap(const ptk_server *s)
+{
+    static const int caps[] = {192, 128, 96, 64, 48, 32, 24, 16, 12, 8};
+    const long long want = 4LL * s->resident;
+    for (int cap : caps) {
+        long long tiles = 0;
+        for (const Inst *in : s->active) {
+            const int d = depth_for_cap(in->L.nz, cap);
+            const int kc = d ? d : in->L.nz;
+            tiles += (long long)((in->L.nx + kTileX - 1) / kTileX) * ((in->L.ny + s->rows - 1) / s->rows) *
+                     ((in->L.nz + kc - 1) / kc);
+        }
+        if (tiles >= want) return cap;
+    }
+    return 8;
+}
+
+InstDesc instance_desc(const ptk_server *s, const Inst *in)
+{
+    InstDesc d{};
+    for (int b = 0; b < 2; ++b)
+        for (int f = 0; f < 6; ++f) d.buf[b][f] = in->buf[b][f];
+    for (int c = 0; c < 4; ++c) d.coef[c] = in->coef[c];
+    d.wave = in->wave;
+    d.plane = in->L.plane;
+    d.nx = in->L.nx; d.ny = in->L.ny; d.nz = in->L.nz; d.pitch = in->L.pitch;
+    d.cx = in->p.Cx; d.cy = in->p.Cy; d.cz = in->p.Cz;
+    d.src = in->nwave ? in->src : -1;
+    d.nwave = in->nwave;
+    d.step = in->done;
+    d.steps_left = in->steps_total - in->done;
+    d.tma = in->tma;
+    plan_tiles(d, s->rows, instance_depth(s, in->L.nz), s->vec);
+    return d;
+}
+
 int admit(ptk_server *s, Inst *in)
 {
     std::vector<BoxSpec> boxes;
@@ -166,6 +228,7 @@ int admit(ptk_server *s, Inst *in)
         for (int f = 0; f < 6 && !rc; ++f) rc = pool_alloc(bytes, st, (void **)&in->buf[b][f]);
     for (int c = 0; c < 4 && !rc; ++c) rc = pool_alloc(bytes, st, (void **)&in->coef[c]);
     if (!rc) rc = pool_alloc(6 * sizeof(double), st, (void **)&in->d_sum);
+    if (!rc && s->stages) rc = pool_alloc(kTmaSetBytes, st, &in->tma);
     in->nwave = (si >= 0 && !wave.empty()) ? (int)wave.size() : 0;
     if (!rc && in->nwave) rc = pool_alloc(wave.size() * sizeof(float), st, (void **)&in->wave);
     if (rc) return rc;
@@ -190,6 +253,13 @@ int admit(ptk_server *s, Inst *in)
         PTK_CUDA_TRY(cudaMemcpyAsync(in->wave, wave.data(), wave.size() * sizeof(float), cudaMemcpyHostToDevice, st));
         in->src = (long long)si + (long long)in->L.pitch * sj + in->L.plane * sk;
     }
+    if (s->stages) {
+        // The arrays never move while the instance lives: its tensor maps are encoded once.
+        alignas(64) unsigned char maps[kTmaSetBytes];
+        rc = encode_tma_set(instance_desc(s, in), s->rows, maps);
+        if (rc) return rc;
+        PTK_CUDA_TRY(cudaMemcpyAsync(in->tma, maps, kTmaSetBytes, cudaMemcpyHostToDevice, st));
+    }
     in->bytes = instance_bytes(in->L, in->nwave);
     s->used += in->bytes;
     s->peak_bytes = std::max(s->peak_bytes, s->used);
@@ -206,6 +276,8 @@ void release(ptk_server *s, Inst *in)
     for (int c = 0; c < 4; ++c) pool_free(in->coef[c], s->st);
     pool_free(in->wave, s->st);
     pool_free(in->d_sum, s->st);
+    pool_free(in->tma, s->st);
+    in->tma = nullptr;
     for (int b = 0; b < 2; ++b)
         for (int f = 0; f < 6; ++f) in->buf[b][f] = nullptr;
     s->used -= in->bytes;
@@ -220,22 +292,17 @@ int rebuild_worklist(ptk_server *s)
     // 128-wide tiles (4 cells per thread): narrower tiles keep more lanes busy on small grids but
     // hold fewer bytes in flight per thread, and measured slower on the batched workload.
     s->vec = 4;
+    if (s->stages) {
+        s->depth_cap = choose_depth_cap(s);
+        // longest tiles first, so that the dynamic tile queue ends with short ones
+        std::stable_sort(s->active.begin(), s->active.end(), [s](const Inst *a, const Inst *b) {
+            const int da = instance_depth(s, a->L.nz), db = instance_depth(s, b->L.nz);
+            return (da ? da : a->L.nz) > (db ? db : b->L.nz);
+        });
+    }
     int tiles = 0;
     for (int q = 0; q < n; ++q) {
-        Inst *in = s->active[q];
-        InstDesc d{};
-        for (int b = 0; b < 2; ++b)
-            for (int f = 0; f < 6; ++f) d.buf[b][f] = in->buf[b][f];
-        for (int c = 0; c < 4; ++c) d.coef[c] = in->coef[c];
-        d.wave = in->wave;
-        d.plane = in->L.plane;
-        d.nx = in->L.nx; d.ny = in->L.ny; d.nz = in->L.nz; d.pitch = in->L.pitch;
-        d.cx = in->p.Cx; d.cy = in->p.Cy; d.cz = in->p.Cz;
-        d.src = in->nwave ? in->src : -1;
-        d.nwave = in->nwave;
-        d.step = in->done;
-        d.steps_left = in->steps_total - in->done;
-        plan_tiles(d, s->cfg.tile_rows, in->L.nz > 48 ? 16 : 0, s->vec);
+        const InstDesc d = instance_desc(s, s->active[q]);
         s->h_desc[q] = d;
         s->h_tile0[q] = tiles;
         tiles += d.tiles_x * d.tiles_y * d.tiles_z + d.face_tiles;
@@ -253,7 +320,7 @@ int rebuild_worklist(ptk_server *s)
 int chunk_graph(ptk_server *s, int len, int grid, cudaGraphExec_t *out)
 {
     const int n = (int)s->active.size();
-    auto key = std::make_tuple(len, n, s->total_tiles, grid * 8 + s->vec);
+    auto key = std::make_tuple(len, n, s->total_tiles, (grid * 8 + s->vec) * 8 + s->stages);
     auto it = s->graphs.find(key);
     if (it != s->graphs.end()) {
         *out = it->second;
@@ -264,8 +331,14 @@ int chunk_graph(ptk_server *s, int len, int grid, cudaGraphExec_t *out)
     PTK_CUDA_TRY(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
     set_capturing(true);
     int rc = PTK_OK;
+    if (s->stages && cudaMemsetAsync(s->d_work, 0, sizeof(int) * len, cap) != cudaSuccess)
+        rc = set_error(PTK_ERR_CUDA, "chunk capture: counter reset failed");
+    else if (s->stages)
+        count_launches(1);
     for (int q = 0; q < len && !rc; ++q)
-        rc = launch_yee_step_v(s->d_desc, s->d_tile0, n, s->total_tiles, q, s->cfg.tile_rows, s->vec, grid, cap);
+        rc = s->stages ? launch_yee_step_bulk(s->d_desc, s->d_tile0, n, s->total_tiles, q, s->rows, s->stages, grid,
+                                              s->d_err, cap, s->d_work)
+                       : launch_yee_step_v(s->d_desc, s->d_tile0, n, s->total_tiles, q, s->rows, s->vec, grid, cap);
     if (!rc) rc = launch_advance(s->d_desc, n, len, cap);
     set_capturing(false);
     cudaGraph_t g = nullptr;
@@ -331,6 +404,31 @@ int ptk_server_create(const ptk_server_config *cfg, ptk_server **out)
     if (s->cfg.max_active <= 0) s->cfg.max_active = 1 << 20;
     if (s->cfg.chunk_steps <= 0) s->cfg.chunk_steps = 32;
     if (s->cfg.tile_rows != 4 && s->cfg.tile_rows != 8 && s->cfg.tile_rows != 16) s->cfg.tile_rows = 8;
+    s->rows = s->cfg.tile_rows;
+    if (s->cfg.stages < 0) {
+        s->stages = 0;
+    } else if (s->cfg.stages == 0) {
+        if (s->rows == 16) s->rows = 8;
+        s->stages = s->rows == 4 ? 3 : 4;
+    } else {
+        s->stages = s->cfg.stages;
+        if (yee_bulk_smem_bytes(s->rows, s->stages) == 0) {
+            delete s;
+            return set_error(PTK_ERR_INVALID, "no staged kernel for %d rows with %d stages", cfg->tile_rows,
+                             cfg->stages);
+        }
+    }
+    if (s->stages && (pool_alloc(sizeof(int), default_stream(), (void **)&s->d_err) ||
+                      pool_alloc(sizeof(int) * s->cfg.chunk_steps, default_stream(), (void **)&s->d_work) ||
+                      cudaMallocHost(&s->h_err, sizeof(int)) != cudaSuccess ||
+                      cudaMemsetAsync(s->d_err, 0, sizeof(int), default_stream()) != cudaSuccess ||
+                      cudaStreamSynchronize(default_stream()) != cudaSuccess)) {
+        if (s->d_err) pool_free(s->d_err, default_stream());
+        if (s->d_work) pool_free(s->d_work, default_stream());
+        if (s->h_err) cudaFreeHost(s->h_err);
+        delete s;
+        return set_error(PTK_ERR_CUDA, "server error word allocation failed");
+    }
     if (s->cfg.hbm_budget_bytes == 0) {
         size_t f = 0, t = 0;
         cudaMemGetInfo(&f, &t);
@@ -379,7 +477,9 @@ int ptk_server_run(ptk_server *s, double time_scale)
     const double t0 = now_s();
     size_t nxt = 0;
     int grid_cap[5] = {0, 0, 0, 0, 0};   // resident CTAs per vec (1, 2, 4)
-    for (int v : {1, 2, 4}) grid_cap[v] = std::max(1, yee_resident_ctas(s->cfg.tile_rows, v));
+    for (int v : {1, 2, 4})
+        grid_cap[v] = std::max(1, s->stages ? yee_bulk_resident_ctas(s->rows, s->stages) : yee_resident_ctas(s->rows, v));
+    s->resident = grid_cap[4];
     auto clock = [&] { return (now_s() - t0); };
     auto arrived = [&](Inst *in, double t) { return time_scale <= 0 || in->t_arrival * time_scale <= t; };
     int rc = PTK_OK;
@@ -420,8 +520,16 @@ int ptk_server_run(ptk_server *s, double time_scale)
         count_graph_launch(len + 1);
         s->launches += len + 1;
         ++s->chunks;
+        if (s->stages && cudaMemcpyAsync(s->h_err, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->st) != cudaSuccess) {
+            rc = set_error(PTK_ERR_CUDA, "error word copy failed");
+            break;
+        }
         if (cudaStreamSynchronize(s->st) != cudaSuccess) {
             rc = set_error(PTK_ERR_CUDA, "chunk failed: %s", cudaGetErrorString(cudaGetLastError()));
+            break;
+        }
+        if (s->stages && *s->h_err) {
+            rc = set_error(PTK_ERR_TIMEOUT, "staged step kernel: a bounded wait expired (error word %d)", *s->h_err);
             break;
         }
         t = clock();
@@ -512,6 +620,9 @@ int ptk_server_destroy(ptk_server *s)
     if (s->d_tile0) pool_free(s->d_tile0, s->st);
     if (s->h_desc) cudaFreeHost(s->h_desc);
     if (s->h_tile0) cudaFreeHost(s->h_tile0);
+    if (s->d_err) pool_free(s->d_err, s->st);
+    if (s->d_work) pool_free(s->d_work, s->st);
+    if (s->h_err) cudaFreeHost(s->h_err);
     cudaStreamSynchronize(s->st);
     cudaStreamDestroy(s->st);
     for (Inst *in : s->all) delete in;

@@ -64,7 +64,7 @@ __host__ __device__ constexpr uint32_t plane_tx_bytes()
 template <int BY>
 __host__ __device__ constexpr size_t xchg_bytes() { return (size_t)2 * 2 * (BY + 1) * 32 * sizeof(float4); }
 template <int BY, int S>
-__host__ __device__ constexpr size_t smem_bytes() { return S * stage_bytes<BY>() + xchg_bytes<BY>() + S * 8; }
+__host__ __device__ constexpr size_t smem_bytes() { return S * stage_bytes<BY>() + xchg_bytes<BY>() + S * 8 + 16; }
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -150,12 +150,13 @@ __device__ __forceinline__ const float *row_ptr(const unsigned char *st, int a, 
 template <int BY, int S>
 __global__ void __launch_bounds__(32 * (BY + 1), 1)
 k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile0, int ninst, int s_off,
-                int total_tiles, int *err)
+                int total_tiles, int *err, int *work)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     unsigned char *stages = smem;
     float4 *xchg = reinterpret_cast<float4 *>(smem + S * stage_bytes<BY>());   // [2 buf][2 arr][BY+1][32]
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + S * stage_bytes<BY>() + xchg_bytes<BY>());
+    int *slot = reinterpret_cast<int *>(bars + S);   // next tile, handed to the whole CTA
 
     const int lane = threadIdx.x, ty = threadIdx.y;
     if (smem_u32(smem) & 127u) {   // TMA destinations need 128-byte alignment: refuse, do not fault
@@ -171,7 +172,17 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
     unsigned gbase = 0;     // planes loaded by this CTA before the current tile
     bool failed = false;
 
-    for (int t = blockIdx.x; t < total_tiles; t += gridDim.x) {
+    // Tiles: the first one is blockIdx.x; later ones are static (t + gridDim.x) or, with a work
+    // counter (zeroed before the launch), taken in list order as CTAs free up.  Every branch that
+    // ends a tile is uniform across the CTA, so the barriers in `advance` are reached by all.
+    auto advance = [&](int t) -> int {
+        if (!work) return t + (int)gridDim.x;
+        __syncthreads();
+        if (ty == 0 && lane == 0) *slot = (int)gridDim.x + atomicAdd(work + s_off, 1);
+        __syncthreads();
+        return *slot;
+    };
+    for (int t = blockIdx.x; t < total_tiles; t = advance(t)) {
         int lo = 0, hi = ninst;
         while (hi - lo > 1) {
             const int mid = (lo + hi) >> 1;
@@ -399,13 +410,14 @@ static int resident_bulk()
 
 template <int BY, int S>
 static int launch_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles, int s_offset,
-                       int grid, int *err, cudaStream_t s)
+                       int grid, int *err, int *work, cudaStream_t s)
 {
     const size_t smem = smem_bytes<BY, S>();
     int rc = prepare_bulk<BY, S>();
     if (rc) return rc;
     const int g = (grid <= 0 || grid > total_tiles) ? total_tiles : grid;
-    k_yee_step_bulk<BY, S><<<g, dim3(32, BY + 1), smem, s>>>(d_insts, d_tile0, ninst, s_offset, total_tiles, err);
+    k_yee_step_bulk<BY, S><<<g, dim3(32, BY + 1), smem, s>>>(d_insts, d_tile0, ninst, s_offset, total_tiles, err,
+                                                             work);
     PTK_CUDA_TRY(cudaGetLastError());
     count_launches(1);
     return PTK_OK;
@@ -414,12 +426,12 @@ static int launch_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, i
 // Rings of at least 2 stages: plane q waits for the stage of plane q+1 before its barrier, and the
 // stage of plane q+1 is issued after the barrier of plane q+1-S, so q+1-S <= q-1.
 int launch_yee_step_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles, int s_offset,
-                         int by, int stages, int grid, int *err, cudaStream_t s)
+                         int by, int stages, int grid, int *err, cudaStream_t s, int *work)
 {
     if (total_tiles <= 0) return PTK_OK;
 #define PTK_BULK(B, S)                                                                                  \
     if (by == B && stages == S)                                                                         \
-        return launch_bulk<B, S>(d_insts, d_tile0, ninst, total_tiles, s_offset, grid, err, s);
+        return launch_bulk<B, S>(d_insts, d_tile0, ninst, total_tiles, s_offset, grid, err, work, s);
     PTK_BULK(4, 2) PTK_BULK(4, 3) PTK_BULK(4, 4) PTK_BULK(4, 5)
     PTK_BULK(8, 2) PTK_BULK(8, 3) PTK_BULK(8, 4)
 #undef PTK_BULK

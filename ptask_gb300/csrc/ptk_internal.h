@@ -103,9 +103,10 @@ int launch_yee_step_v(const InstDesc *d_insts, const int *d_tile0, int ninst, in
                       int by, int vec, int grid, cudaStream_t s);
 // The staged variant (operands brought into shared memory by TMA tensor copies, `stages` planes
 // in a ring; 128-wide tiles, vec == 4; every instance's `tma` set encoded for `by`).  *err is
-// raised if a bounded wait expires.
+// raised if a bounded wait expires.  With `work` (one zeroed counter per step offset), CTAs past
+// the first wave take tiles in list order as they free up instead of a static stride.
 int launch_yee_step_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles, int s_offset,
-                         int by, int stages, int grid, int *err, cudaStream_t s);
+                         int by, int stages, int grid, int *err, cudaStream_t s, int *work = nullptr);
 size_t yee_bulk_smem_bytes(int by, int stages);
 // CTAs of the staged kernel that fit on the whole GPU at once (0: no such kernel).
 int yee_bulk_resident_ctas(int by, int stages);

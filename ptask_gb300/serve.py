@@ -65,10 +65,13 @@ class Server:
     """Continuous-batching FDTD server (max_active=1 gives plain one-at-a-time dispatch)."""
 
     def __init__(self, budget_bytes: int = 0, max_active: int = 0, chunk_steps: int = 32, tile_rows: int = 8,
-                 keep_results: bool = False, persistent: bool = True):
+                 keep_results: bool = False, persistent: bool = True, stages: int = 0):
+        """`stages`: 0 = TMA-staged step kernel with its default ring, 2..5 = that many planes,
+        -1 = register kernel."""
         lib()
         self._h = C.c_void_p()
-        self.cfg = ServerConfig(budget_bytes, max_active, chunk_steps, tile_rows, int(keep_results), int(persistent))
+        self.cfg = ServerConfig(budget_bytes, max_active, chunk_steps, tile_rows, int(keep_results), int(persistent),
+                                stages)
         call("ptk_server_create", C.byref(self.cfg), C.byref(self._h))
         self.requests: list[Request] = []
 
@@ -108,3 +111,69 @@ class Server:
 
     def __exit__(self, *a):
         self.close()
+
+
+def graph_dispatch(reqs: list[Request], time_scale: float = 1.0, mode: str = "taskwise",
+                   cache: int = 4, results: dict | None = None) -> dict:
+    """Plain per-graph dispatch of the same requests: one PTask FDTD graph per request shape
+    (ptaskUnitTest/graphfdtd.cpp builds one graph per problem size), run one request at a time in
+    arrival order.  Each request pushes its coefficients and zero fields into the graph, runs its
+    steps and pulls the six fields back, as the reference's graph driver does
+    (graphfdtd.cpp:1076-1125).  `mode` "taskwise" dispatches the H and E tasks of every iteration
+    one by one through the scheduler (the reference's model); "fused" lowers the cycle to the
+    fused loop.  The next request's problem is generated on the host while the current one runs.
+    Returns wall time, solves, p50/p99 latency (finish minus arrival x time_scale); with `results`
+    given, also stores each request's six fields under its index."""
+    import threading
+    import time
+    from collections import OrderedDict
+
+    from .fdtd import Problem
+    from .graph import FDTDGraph
+
+    def make(r: Request) -> Problem:
+        return Problem.generate(r.nx, r.ny, r.nz, n_boxes=r.n_boxes, eps=r.eps, box=r.box, courant=0.5,
+                                steps=r.steps, source_mode=r.source_mode, seed=r.seed)
+
+    order = sorted(range(len(reqs)), key=lambda q: reqs[q].arrival)
+    slot: dict = {}
+
+    def prefetch(q: int) -> threading.Thread:
+        th = threading.Thread(target=lambda: slot.__setitem__(q, make(reqs[q])))
+        th.start()
+        return th
+
+    graphs: OrderedDict = OrderedDict()
+    lat = []
+    pending = prefetch(order[0]) if order else None
+    t0 = time.perf_counter()
+    try:
+        for n, q in enumerate(order):
+            r = reqs[q]
+            pending.join()
+            prob = slot.pop(q)
+            pending = prefetch(order[n + 1]) if n + 1 < len(order) else None
+            wait = r.arrival * time_scale - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(wait)
+            key = (r.nx, r.ny, r.nz)
+            g = graphs.pop(key, None)
+            if g is None:
+                g = FDTDGraph(prob.params, mode=mode)
+                while len(graphs) >= cache:
+                    graphs.popitem(last=False)[1].close()
+            graphs[key] = g
+            g.set_problem(prob)
+            out = g.solve(zero_fields(r.nx, r.ny, r.nz), r.steps)
+            if results is not None:
+                results[q] = out
+            lat.append(time.perf_counter() - t0 - r.arrival * time_scale)
+        wall = time.perf_counter() - t0
+    finally:
+        if pending is not None:
+            pending.join()
+        for g in graphs.values():
+            g.close()
+    lat_s = sorted(lat)
+    pick = (lambda f: lat_s[min(len(lat_s) - 1, int(f * len(lat_s)))]) if lat_s else (lambda f: 0.0)
+    return {"wall_s": wall, "solves": len(lat), "p50_latency_s": pick(0.50), "p99_latency_s": pick(0.99)}

@@ -5,7 +5,7 @@ import pytest
 
 import oracle
 import ptask_gb300 as P
-from ptask_gb300.serve import Request, Server, batched_instances, poisson_trace
+from ptask_gb300.serve import Request, Server, batched_instances, graph_dispatch, poisson_trace
 
 pytestmark = pytest.mark.gpu
 
@@ -17,10 +17,12 @@ def alone(r: Request):
     return P.solve(pr, P.zero_fields(r.nx, r.ny, r.nz), r.steps), pr
 
 
-def test_mixed_batch_results_equal_alone():
+@pytest.mark.parametrize("rows,stages", [(8, 0), (8, -1), (4, 3), (8, 2)])
+def test_mixed_batch_results_equal_alone(rows, stages):
+    """Staged (default ring, 2-plane ring, 4 rows) and register kernels all give the solo results."""
     reqs = [Request(24, 20, 16, 40, 2, 1), Request(37, 29, 23, 75, 3, 2), Request(64, 48, 40, 33, 1, 3),
-            Request(17, 33, 9, 61, 2, 4), Request(130, 24, 20, 20, 4, 5)]
-    with Server(keep_results=True, chunk_steps=16) as s:
+            Request(17, 33, 9, 61, 2, 4), Request(130, 24, 20, 20, 4, 5), Request(40, 36, 230, 9, 3, 6)]
+    with Server(keep_results=True, chunk_steps=16, tile_rows=rows, stages=stages) as s:
         tickets = [s.submit(r) for r in reqs]
         s.run(time_scale=0)
         st = s.stats()
@@ -70,10 +72,31 @@ def test_continuous_admission_within_budget_and_plain_mode_agrees():
                 np.testing.assert_array_equal(got[q], batched[t][q])
 
 
+def test_plain_graph_dispatch_matches_server():
+    """The per-graph plain arm (one task-wise PTask graph per request) gives the server's results."""
+    reqs = poisson_trace(6, rate=2000.0, seed=13, edge=(12, 40), steps=(10, 40))
+    reqs.append(Request(reqs[0].nx, reqs[0].ny, reqs[0].nz, 17, 2, 77, arrival=reqs[-1].arrival))  # graph reuse
+    got: dict = {}
+    st = graph_dispatch(reqs, time_scale=1.0, mode="taskwise", cache=2, results=got)
+    assert st["solves"] == len(reqs) and st["p99_latency_s"] >= st["p50_latency_s"] >= 0
+    with Server(keep_results=True, chunk_steps=8) as s:
+        tickets = [s.submit(r) for r in reqs]
+        s.run(time_scale=0)
+        for q, t in enumerate(tickets):
+            ref = s.fetch(t)
+            for f in range(6):
+                np.testing.assert_array_equal(got[q][f], ref[f], err_msg=f"request {q} field {P.FIELDS[f]}")
+
+
 def test_request_larger_than_budget_is_rejected():
     with Server(budget_bytes=1 << 20) as s:
         with pytest.raises(P.PtkError):
             s.submit(Request(64, 64, 64, 10, 1, 1))
+
+
+def test_server_rejects_unknown_staged_shape():
+    with pytest.raises(P.PtkError):
+        Server(tile_rows=16, stages=3)
 
 
 def test_batched_config_generator_shapes():
