@@ -40,14 +40,14 @@ BYTES_PER_CELL = 64          # 6 fields read + written (48 B) + 4 coefficients r
 FALLBACK_HBM_GBS = 6800.0
 
 WORKLOADS = {
-    # BASELINE configs[1]
+    # the plain-graph headline workload
     "plain256": dict(shape=(256, 256, 256), boxes=8, eps=(1.0, 10.0), box=(8, 64), steps=1000,
                      desc="plain FDTD graph 256^3 FP32, 8 seeded dielectric boxes (eps_r 1-10, edges 8-64), "
                           "PEC walls, Courant 0.5, Gaussian Ez source at centre, 1000 steps"),
-    # BASELINE configs[2]
+    # the large single-GPU workload
     "large": dict(shape=(512, 512, 384), boxes=32, eps=(1.0, 10.0), box=(8, 64), steps=500,
                   desc="large plain FDTD 512x512x384 FP32, 32 seeded dielectric boxes, 500 steps"),
-    # BASELINE configs[0] (the CPU-runnable case), used for quick checks
+    # the CPU-runnable case, used for quick checks
     "cpu32": dict(shape=(32, 32, 32), boxes=2, eps=(2.0, 6.0), box=(4, 16), steps=100,
                   desc="32^3 FP32, 2 dielectric boxes (eps_r 2-6), 100 steps"),
 }

@@ -218,6 +218,21 @@ def test_full_size_first_steps_match_oracle(full_problem):
     assert_parity(got, ref, "256^3 x 3")
 
 
+def test_full_size_full_length_matches_oracle(full_problem):
+    """The plain-graph workload itself (256^3, 1000 steps from zero fields) with the autotuned
+    tiles, bit for bit against the FP32 oracle."""
+    pr = full_problem
+    f = P.zero_fields(*FULL)
+    with P.Solver(pr.params) as s:
+        s.set_tiles(*P.tuned_tiles(*FULL))
+        s.set_fields(f)
+        s.set_problem(pr)
+        s.run(1000)
+        got = s.get_fields()
+    ref = oracle.step_ext_f32(f, 1000, pr.params, pr.Ca, pr.Cb, pr.Da, pr.Db, pr.src, pr.wave)
+    assert_parity(got, ref, "256^3 x 1000")
+
+
 def test_full_size_tiling_and_chunking_invariance(full_problem):
     pr = full_problem
     f = P.zero_fields(*FULL)
