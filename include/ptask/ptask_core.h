@@ -163,6 +163,9 @@ public:
     void SetSticky(BOOL b) { m_sticky_flag = b; }
     BOOL IsOccupied();
     UINT GetChannelCount() { return (UINT)(m_type == OUTPUT_PORT ? m_out.size() : m_in.size()); }
+    // Position in the port array passed to Graph::AddTask (port.h GetOriginalIndex/SetOriginalIndex).
+    UINT GetOriginalIndex() { return m_orig_idx; }
+    void SetOriginalIndex(UINT i) { m_orig_idx = i; }
     Channel *GetChannel(UINT i);
 
     // ---- runtime side ----
@@ -182,6 +185,7 @@ private:
     int m_inout_idx;
     METAFUNCTION m_meta = MF_NONE;
     BOOL m_sticky_flag = FALSE;
+    UINT m_orig_idx = 0;
 };
 
 class InputPort : public Port {
@@ -296,6 +300,7 @@ public:
     void SetComputeGeometry(int x = 1, int y = 1, int z = 1);
     void SetBlockAndGridSize(PTASKDIM3 grid, PTASKDIM3 block);
     const char *GetTaskName() { return m_name.c_str(); }
+    ACCELERATOR_CLASS GetAcceleratorClass() { return ACCELERATOR_CLASS_CUDA; }
     Graph *GetGraph() { return m_graph; }
     CompiledKernel *GetCompiledKernel() { return m_kernel; }
     UINT GetInputPortCount() { return (UINT)m_inputs.size(); }
@@ -308,6 +313,7 @@ public:
     std::vector<Port *> m_inputs;
     std::vector<Port *> m_outputs;
     PTASKDIM3 m_geom, m_grid, m_block;
+    bool m_geom_set = false;
     bool m_explicit_launch = false;
     UINT64 m_dispatches = 0;
     // MF_GENERAL_ITERATOR state of a meta port on this task
@@ -363,6 +369,14 @@ public:
     void BindControlPort(Port *pController, Port *pGatedPort, BOOL bInitiallyOpen = FALSE);
     PTRESULT CheckGraphSemantics(BOOL bVerbose = TRUE, BOOL bFixErrors = TRUE);
     const char *GetName() { return m_name.c_str(); }
+    Channel *GetChannel(const char *lpszChannelName);
+    Task *GetTask(const char *lpszTaskName);
+    // Graph structure to / from an XML file in the reference's format (graph.h:1545, :1561;
+    // XMLWriter.cpp, XMLReader.cpp).  Deserialize builds into an empty graph.
+    void Serialize(const char *filename);
+    void Deserialize(const char *filename);
+    // GB300 extension: why the last Serialize / Deserialize failed ("" after a success).
+    const char *GetSerializationError() { return m_xml_error.c_str(); }
 
     // ---- GB300 extensions ----
     // Lower MF_GENERAL_ITERATOR loops to a captured CUDA graph / registered fused kernel (default on).
@@ -375,6 +389,13 @@ public:
 
     // ---- runtime side ----
     void Signal();                 // a channel changed: wake the scheduler
+    // Bindings kept for serialization (the FDTD path does not act on them).
+    struct ControlPortBinding { Port *controller, *gated; BOOL open; };
+    struct DescriptorBinding { Port *described, *describer; DESCRIPTORFUNC func; };
+    std::vector<std::pair<Port *, Channel *>> m_ctl_channels;   // BindControlPropagationChannel
+    std::vector<std::pair<Port *, Port *>> m_iter_scopes;       // BindIterationScope
+    std::vector<DescriptorBinding> m_descriptors;               // BindDescriptorPort
+    std::vector<ControlPortBinding> m_control_ports;            // BindControlPort
     std::vector<Task *> m_tasks;
     std::vector<Channel *> m_channels;
     std::vector<Port *> m_ports;
@@ -405,6 +426,7 @@ private:
     GraphStats m_stats;
     std::vector<std::unique_ptr<CyclePlan>> m_plans;
     bool m_finalized = false;
+    std::string m_xml_error;
 };
 
 // ---------------------------------------------------------------------------------------------

@@ -72,6 +72,30 @@ int ptk_fdtd_graph_write_dot(ptk_fdtd_graph *g, const char *path);
 /* Graph::Stop, Teardown, DestroyGraph (ptask/graph.h:234, :242, :122). */
 int ptk_fdtd_graph_destroy(ptk_fdtd_graph *g);
 
+/* ---- graph files (Graph::Serialize / Graph::Deserialize, ptask/graph.h:1545, :1561) ----------
+ * The file holds the graph's structure in the reference's XML layout (ptask/XMLWriter.cpp,
+ * XMLReader.cpp): templates, kernels, tasks and ports, channels and configuration actions. */
+
+/* Write the running graph's structure.  PTK_ERR_STATE if the file cannot be written. */
+int ptk_fdtd_graph_save(ptk_fdtd_graph *g, const char *path);
+
+/* Build and start an FDTD graph from a file written by ptk_fdtd_graph_save or by the reference's
+ * Graph::Serialize.  The file decides the structure (unrolled per-field tasks or the cyclic pair);
+ * for a cyclic file `mode` chooses the lowering (FUSED, CAPTURED or TASKWISE) and
+ * PTK_GRAPH_UNROLLED is rejected.  `p` supplies FDTD_PARAMS, which a graph file does not hold; the
+ * field templates in the file must match its grid.  Boundary channels are found by the template and
+ * variable binding of their ports.  PTK_ERR_STATE: unreadable or malformed file;
+ * PTK_ERR_INVALID: not an FDTD graph for this grid. */
+int ptk_fdtd_graph_load(const ptk_fdtd_params *p, int mode, const char *path, ptk_fdtd_graph **out);
+
+/* Write the structure of the graph ptk_fdtd_graph_create would build, without starting it (no
+ * device needed). */
+int ptk_fdtd_graph_export(const ptk_fdtd_params *p, int mode, int unrolled_steps, const char *path);
+
+/* Read any graph file into a new graph and write it out again (no device needed): the output
+ * equals the input for files written by this runtime. */
+int ptk_graph_xml_roundtrip(const char *in_path, const char *out_path);
+
 #ifdef __cplusplus
 }
 #endif

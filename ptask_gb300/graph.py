@@ -34,6 +34,10 @@ _SIGS = {
     "ptk_fdtd_graph_stats": [_P, C.POINTER(GraphStats)],
     "ptk_fdtd_graph_write_dot": [_P, C.c_char_p],
     "ptk_fdtd_graph_destroy": [_P],
+    "ptk_fdtd_graph_save": [_P, C.c_char_p],
+    "ptk_fdtd_graph_load": [C.POINTER(FdtdParams), C.c_int, C.c_char_p, C.POINTER(_P)],
+    "ptk_fdtd_graph_export": [C.POINTER(FdtdParams), C.c_int, C.c_int, C.c_char_p],
+    "ptk_graph_xml_roundtrip": [C.c_char_p, C.c_char_p],
 }
 
 
@@ -59,12 +63,28 @@ def _check(rc: int, where: str) -> None:
 class FDTDGraph:
     """The FDTD task graph on the PTask runtime (see ptask_graph.h for the forms)."""
 
-    def __init__(self, params: FdtdParams, mode: str = "fused", unrolled_steps: int = 0):
+    def __init__(self, params: FdtdParams, mode: str = "fused", unrolled_steps: int = 0, *, _handle=None):
         self.params = params
         self.mode = mode
         self._h = C.c_void_p()
+        if _handle is not None:
+            self._h = _handle
+            return
         _check(rt().ptk_fdtd_graph_create(C.byref(params), MODES[mode], unrolled_steps, C.byref(self._h)),
                "ptk_fdtd_graph_create")
+
+    @classmethod
+    def load(cls, params: FdtdParams, path, mode: str = "fused") -> "FDTDGraph":
+        """A graph built from a graph file (Graph::Deserialize); `mode` is the lowering of a cyclic
+        file and ignored for an unrolled one."""
+        h = C.c_void_p()
+        _check(rt().ptk_fdtd_graph_load(C.byref(params), MODES[mode], str(path).encode(), C.byref(h)),
+               "ptk_fdtd_graph_load")
+        return cls(params, mode, _handle=h)
+
+    def save(self, path) -> None:
+        """Write the graph's structure (Graph::Serialize)."""
+        _check(rt().ptk_fdtd_graph_save(self._h, str(path).encode()), "ptk_fdtd_graph_save")
 
     def set_problem(self, prob: Problem | None) -> None:
         if prob is None:
@@ -111,3 +131,14 @@ class FDTDGraph:
 
     def __exit__(self, *a):
         self.close()
+
+
+def export_graph(params: FdtdParams, path, mode: str = "fused", unrolled_steps: int = 0) -> None:
+    """Write the structure of the FDTD graph of `mode` without starting it (no device needed)."""
+    _check(rt().ptk_fdtd_graph_export(C.byref(params), MODES[mode], unrolled_steps, str(path).encode()),
+           "ptk_fdtd_graph_export")
+
+
+def xml_roundtrip(in_path, out_path) -> None:
+    """Read a graph file into a new graph and write it out again (no device needed)."""
+    _check(rt().ptk_graph_xml_roundtrip(str(in_path).encode(), str(out_path).encode()), "ptk_graph_xml_roundtrip")

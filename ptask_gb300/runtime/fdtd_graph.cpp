@@ -181,16 +181,9 @@ int push_copy(GraphInputChannel *c, DatablockTemplate *t, const void *data, size
     return ok ? PTK_OK : PTK_ERR_TIMEOUT;
 }
 
-}  // namespace
-
-extern "C" {
-
-int ptk_fdtd_graph_create(const ptk_fdtd_params *p, int mode, int unrolled_steps, ptk_fdtd_graph **out)
+// Wrapper with the FDTD templates of `p` and an empty graph (no device work).
+ptk_fdtd_graph *new_graph(const ptk_fdtd_params *p, int mode, int unrolled_steps)
 {
-    if (!p || !out || p->Nx < 1 || p->Ny < 1 || p->Nz < 1 || mode < 0 || mode > 3) return PTK_ERR_INVALID;
-    if (mode == PTK_GRAPH_UNROLLED && unrolled_steps < 1) return PTK_ERR_INVALID;
-    Runtime::SetExitOnRuntimeFailure(FALSE);
-    if (PTFAILED(Runtime::Initialize())) return PTK_ERR_CUDA;
     auto *G = new ptk_fdtd_graph();
     G->p = *p;
     G->mode = mode;
@@ -205,17 +198,163 @@ int ptk_fdtd_graph_create(const ptk_fdtd_params *p, int mode, int unrolled_steps
     G->src_t = Runtime::GetDatablockTemplate("fdtdsource", sizeof(SourceDesc), PTPARM_BYVALSTRUCT);
     G->iter_t = Runtime::GetDatablockTemplate("dbiter", sizeof(int), PTPARM_INT);
     G->g = new Graph(mode == PTK_GRAPH_UNROLLED ? "graphfdtd_unrolled" : "graphfdtd_cyclic");
-    if (mode == PTK_GRAPH_UNROLLED) build_unrolled(G, unrolled_steps);
-    else build_cyclic(G);
-    G->g->SetCycleLowering(mode != PTK_GRAPH_CYCLIC_TASKWISE);
-    G->g->SetCycleFusion(mode == PTK_GRAPH_CYCLIC_FUSED);
+    return G;
+}
+
+// Lowering choice, Run, and the FDTD_PARAMS block shared by every sticky Config port
+// (graphfdtd.cpp:1099-1104).
+void start(ptk_fdtd_graph *G)
+{
+    G->g->SetCycleLowering(G->mode != PTK_GRAPH_CYCLIC_TASKWISE);
+    G->g->SetCycleFusion(G->mode == PTK_GRAPH_CYCLIC_FUSED);
     G->g->Run(FALSE);
-    // The FDTD_PARAMS block is shared by every sticky Config port (graphfdtd.cpp:1099-1104).
-    Datablock *cp = Runtime::AllocateDatablock(G->param_t, G->p.Nx ? (void *)&G->p : nullptr, sizeof(G->p), nullptr);
+    Datablock *cp = Runtime::AllocateDatablock(G->param_t, (void *)&G->p, sizeof(G->p), nullptr);
     for (GraphInputChannel *c : G->param_in) c->Push(cp);
     cp->Release();
+}
+
+// Find the FDTD graph's boundary channels in a graph read from a file.  Channels are recognised by
+// the template and variable binding of the port they feed or drain, not by name: the reference's
+// driver names its channels differently (graphfdtd.cpp:617-700) from this runtime's builder.
+int bind_loaded(ptk_fdtd_graph *G, int mode)
+{
+    int cyclic = 0, unrolled = 0;
+    for (Task *t : G->g->m_tasks) {
+        const std::string op = t->GetCompiledKernel()->GetOperation();
+        if (op == "FDTDHStep" || op == "FDTDEStep") ++cyclic;
+        else if (op.size() > 11 && op.compare(op.size() - 11, 11, "Computation") == 0) ++unrolled;
+        else return PTK_ERR_INVALID;
+    }
+    if ((cyclic == 0) == (unrolled == 0) || unrolled % 6 || (cyclic && cyclic != 2)) return PTK_ERR_INVALID;
+    if (unrolled) {
+        G->mode = PTK_GRAPH_UNROLLED;
+        G->unrolled_steps = unrolled / 6;
+    } else {
+        if (mode == PTK_GRAPH_UNROLLED) return PTK_ERR_INVALID;
+        G->mode = mode;
+    }
+    auto field_of = [&](DatablockTemplate *t) {
+        for (int f = 0; f < 6; ++f)
+            if (t && !strcmp(t->GetTemplateName(), kTemplateNames[f])) return f;
+        return -1;
+    };
+    for (Channel *c : G->g->m_channels) {
+        if (c->GetType() == CT_GRAPH_INPUT) {
+            Port *d = c->GetBoundPort(CE_DST);
+            DatablockTemplate *t = d->GetTemplate();
+            const std::string tn = t ? t->GetTemplateName() : "", vb = d->GetVariableBinding();
+            auto *in = static_cast<GraphInputChannel *>(c);
+            const int f = field_of(t);
+            if (f >= 0) {
+                if (t->GetXElementCount() != G->field_t[f]->GetXElementCount() ||
+                    t->GetYElementCount() != G->field_t[f]->GetYElementCount() ||
+                    t->GetZElementCount() != G->field_t[f]->GetZElementCount())
+                    return PTK_ERR_INVALID;   // the file was written for another grid
+                G->field_in[f].push_back(in);
+            } else if (tn == "fdtdparms") {
+                G->param_in.push_back(in);
+            } else if (tn == "CellCoef") {
+                static const char *names[4] = {"Ca", "Cb", "Da", "Db"};
+                int q = 0;
+                while (q < 4 && vb != names[q]) ++q;
+                if (q == 4) return PTK_ERR_INVALID;
+                G->coef_in[q] = in;
+            } else if (tn == "fdtdsource") {
+                G->src_in = in;
+            } else if (tn == "fdtdwave") {
+                G->wave_in = in;
+            } else if (tn == "dbiter") {
+                G->iter_in = in;
+            } else {
+                return PTK_ERR_INVALID;
+            }
+        } else if (c->GetType() == CT_GRAPH_OUTPUT) {
+            const int f = field_of(c->GetBoundPort(CE_SRC)->GetTemplate());
+            if (f < 0 || G->field_out[f]) return PTK_ERR_INVALID;
+            G->field_out[f] = static_cast<GraphOutputChannel *>(c);
+        }
+    }
+    for (int f = 0; f < 6; ++f)
+        if (G->field_in[f].empty() || !G->field_out[f]) return PTK_ERR_INVALID;
+    if (G->param_in.empty()) return PTK_ERR_INVALID;
+    if (G->mode != PTK_GRAPH_UNROLLED &&
+        (!G->coef_in[0] || !G->coef_in[1] || !G->coef_in[2] || !G->coef_in[3] || !G->src_in || !G->wave_in ||
+         !G->iter_in))
+        return PTK_ERR_INVALID;
+    return PTK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ptk_fdtd_graph_create(const ptk_fdtd_params *p, int mode, int unrolled_steps, ptk_fdtd_graph **out)
+{
+    if (!p || !out || p->Nx < 1 || p->Ny < 1 || p->Nz < 1 || mode < 0 || mode > 3) return PTK_ERR_INVALID;
+    if (mode == PTK_GRAPH_UNROLLED && unrolled_steps < 1) return PTK_ERR_INVALID;
+    Runtime::SetExitOnRuntimeFailure(FALSE);
+    if (PTFAILED(Runtime::Initialize())) return PTK_ERR_CUDA;
+    ptk_fdtd_graph *G = new_graph(p, mode, unrolled_steps);
+    if (mode == PTK_GRAPH_UNROLLED) build_unrolled(G, unrolled_steps);
+    else build_cyclic(G);
+    start(G);
     *out = G;
     return PTK_OK;
+}
+
+int ptk_fdtd_graph_export(const ptk_fdtd_params *p, int mode, int unrolled_steps, const char *path)
+{
+    if (!p || !path || p->Nx < 1 || p->Ny < 1 || p->Nz < 1 || mode < 0 || mode > 3) return PTK_ERR_INVALID;
+    if (mode == PTK_GRAPH_UNROLLED && unrolled_steps < 1) return PTK_ERR_INVALID;
+    Runtime::SetExitOnRuntimeFailure(FALSE);
+    ptk_fdtd_graph *G = new_graph(p, mode, unrolled_steps);
+    if (mode == PTK_GRAPH_UNROLLED) build_unrolled(G, unrolled_steps);
+    else build_cyclic(G);
+    G->g->Serialize(path);
+    const int rc = *G->g->GetSerializationError() ? PTK_ERR_STATE : PTK_OK;
+    Graph::DestroyGraph(G->g);
+    delete G;
+    return rc;
+}
+
+int ptk_fdtd_graph_save(ptk_fdtd_graph *G, const char *path)
+{
+    if (!G || !path) return PTK_ERR_INVALID;
+    G->g->Serialize(path);
+    return *G->g->GetSerializationError() ? PTK_ERR_STATE : PTK_OK;
+}
+
+int ptk_fdtd_graph_load(const ptk_fdtd_params *p, int mode, const char *path, ptk_fdtd_graph **out)
+{
+    if (!p || !path || !out || p->Nx < 1 || p->Ny < 1 || p->Nz < 1 || mode < 0 || mode > 3) return PTK_ERR_INVALID;
+    Runtime::SetExitOnRuntimeFailure(FALSE);
+    if (PTFAILED(Runtime::Initialize())) return PTK_ERR_CUDA;
+    ptk_fdtd_graph *G = new_graph(p, mode, 0);
+    G->g->Deserialize(path);
+    int rc = *G->g->GetSerializationError() ? PTK_ERR_STATE : bind_loaded(G, mode);
+    if (rc) {
+        Graph::DestroyGraph(G->g);
+        delete G;
+        return rc;
+    }
+    start(G);
+    *out = G;
+    return PTK_OK;
+}
+
+int ptk_graph_xml_roundtrip(const char *in_path, const char *out_path)
+{
+    if (!in_path || !out_path) return PTK_ERR_INVALID;
+    Runtime::SetExitOnRuntimeFailure(FALSE);
+    Graph *g = new Graph("roundtrip");
+    g->Deserialize(in_path);
+    int rc = *g->GetSerializationError() ? PTK_ERR_STATE : PTK_OK;
+    if (!rc) {
+        g->Serialize(out_path);
+        if (*g->GetSerializationError()) rc = PTK_ERR_STATE;
+    }
+    Graph::DestroyGraph(g);
+    return rc;
 }
 
 int ptk_fdtd_graph_set_problem(ptk_fdtd_graph *G, const float *Ca, const float *Cb, const float *Da, const float *Db,

@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cstdlib>
+#include <cstring>
 #include <fstream>
 
 #include "PTaskRuntime.h"
@@ -190,7 +191,11 @@ Task::~Task()
     if (m_step_counter) ptk_mem_free(m_step_counter, m_graph ? m_graph->GetStream() : nullptr);
 }
 
-void Task::SetComputeGeometry(int x, int y, int z) { m_geom = PTASKDIM3(x, y, z); }
+void Task::SetComputeGeometry(int x, int y, int z)
+{
+    m_geom = PTASKDIM3(x, y, z);
+    m_geom_set = true;
+}
 
 void Task::SetBlockAndGridSize(PTASKDIM3 grid, PTASKDIM3 block)
 {
@@ -311,11 +316,13 @@ Task *Graph::AddTask(CompiledKernel *k, UINT nin, Port **in, UINT nout, Port **o
     Task *t = new Task(this, k, name);
     for (UINT i = 0; i < nin; ++i) {
         in[i]->m_task = t;
+        in[i]->SetOriginalIndex(i);
         t->m_inputs.push_back(in[i]);
         m_ports.push_back(in[i]);
     }
     for (UINT i = 0; i < nout; ++i) {
         out[i]->m_task = t;
+        out[i]->SetOriginalIndex(i);
         t->m_outputs.push_back(out[i]);
         m_ports.push_back(out[i]);
     }
@@ -361,10 +368,36 @@ void Graph::BindControlPropagationPort(Port *in, Port *out)
     if (in && out) in->m_ctl_targets.push_back(out);
 }
 
-void Graph::BindControlPropagationChannel(Port *, Channel *) {}
-void Graph::BindIterationScope(Port *, Port *) {}
-void Graph::BindDescriptorPort(Port *, Port *, DESCRIPTORFUNC) {}
-void Graph::BindControlPort(Port *, Port *, BOOL) {}
+void Graph::BindControlPropagationChannel(Port *in, Channel *c)
+{
+    if (in && c) m_ctl_channels.push_back({in, c});
+}
+void Graph::BindIterationScope(Port *meta, Port *scoped)
+{
+    if (meta && scoped) m_iter_scopes.push_back({meta, scoped});
+}
+void Graph::BindDescriptorPort(Port *described, Port *describer, DESCRIPTORFUNC f)
+{
+    if (described && describer) m_descriptors.push_back({described, describer, f});
+}
+void Graph::BindControlPort(Port *controller, Port *gated, BOOL open)
+{
+    if (controller && gated) m_control_ports.push_back({controller, gated, open});
+}
+
+Channel *Graph::GetChannel(const char *name)
+{
+    for (Channel *c : m_channels)
+        if (name && !strcmp(c->GetName(), name)) return c;
+    return nullptr;
+}
+
+Task *Graph::GetTask(const char *name)
+{
+    for (Task *t : m_tasks)
+        if (name && !strcmp(t->GetTaskName(), name)) return t;
+    return nullptr;
+}
 
 PTRESULT Graph::CheckGraphSemantics(BOOL verbose, BOOL)
 {

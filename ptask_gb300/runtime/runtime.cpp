@@ -89,7 +89,7 @@ const char *ViewPolicyString(VIEWMATERIALIZATIONPOLICY p)
 // ---------------------------------------------------------------------------------------------
 DatablockTemplate::DatablockTemplate(const char *name, UINT stride, UINT x, UINT y, UINT z, bool record,
                                      bool raw)
-    : m_name(name ? name : ""), m_stride(stride), m_dims{x, y, z}, m_parm(PTPARM_BUFFER), m_record(record),
+    : m_name(name ? name : ""), m_stride(stride), m_dims{x, y, z}, m_parm(PTPARM_NONE), m_record(record),
       m_raw(raw)
 {
 }

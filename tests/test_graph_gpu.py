@@ -92,3 +92,64 @@ def test_cyclic_one_iteration_and_pipelining():
     ref5 = oracle.step_ext_f32(f, 5, pr.params, pr.Ca, pr.Cb, pr.Da, pr.Db, pr.src, pr.wave)
     for r in many:
         assert_same(r, ref5, "pipelined cyclic")
+
+
+# ------------------------------------------------------------------------------------------------
+# Graph files: a saved graph, loaded into a new graph, computes the same results.
+# ------------------------------------------------------------------------------------------------
+def test_saved_unrolled_graph_loads_and_runs(tmp_path):
+    shape, steps = (24, 20, 6), 3
+    p = P.reference_params(*shape)
+    f = P.random_fields(*shape, seed=61)
+    path = tmp_path / "unrolled.xml"
+    with FDTDGraph(p, "unrolled", unrolled_steps=steps) as g:
+        g.save(path)
+        first = g.solve(f, steps)
+    with FDTDGraph.load(p, path) as g:
+        again = g.solve(f, steps)
+        assert g.stats()["dispatches"] == 6 * steps
+    ref = oracle.step_ref_f32(f, steps, p)
+    assert_same(first, ref, "original")
+    assert_same(again, ref, "loaded")
+
+
+@pytest.mark.parametrize("mode", ["fused", "taskwise"])
+def test_saved_cyclic_graph_loads_in_any_lowering(tmp_path, mode):
+    shape, steps = (33, 21, 17), 29
+    pr = P.Problem.generate(*shape, n_boxes=3, eps=(1, 10), box=(4, 12), steps=steps, seed=8)
+    f = P.random_fields(*shape, seed=62, scale=1e-3)
+    path = tmp_path / "cyclic.xml"
+    with FDTDGraph(pr.params, "captured") as g:
+        g.save(path)
+    with FDTDGraph.load(pr.params, path, mode) as g:
+        g.set_problem(pr)
+        got = g.solve(f, steps)
+        st = g.stats()
+    assert_same(got, oracle.step_ext_f32(f, steps, pr.params, pr.Ca, pr.Cb, pr.Da, pr.Db, pr.src, pr.wave),
+                "loaded " + mode)
+    assert (st["cycles_lowered"] == 1) == (mode == "fused")
+
+
+def test_reference_layout_file_runs(tmp_path):
+    """A file with only the reference's action kinds, its whitespace and foreign channel names."""
+    from test_graph_xml import reference_style
+    from ptask_gb300.graph import export_graph
+    shape, steps = (16, 12, 5), 2
+    p = P.reference_params(*shape)
+    src, ref_file = tmp_path / "ours.xml", tmp_path / "ref.xml"
+    export_graph(p, src, "unrolled", steps)
+    ref_file.write_text(reference_style(src.read_text()))
+    f = P.random_fields(*shape, seed=63)
+    with FDTDGraph.load(p, ref_file) as g:
+        got = g.solve(f, steps)
+    assert_same(got, oracle.step_ref_f32(f, steps, p), "reference-layout file")
+
+
+def test_load_rejects_a_file_for_another_grid(tmp_path):
+    path = tmp_path / "g.xml"
+    from ptask_gb300.graph import export_graph
+    export_graph(P.reference_params(8, 8, 8), path, "fused")
+    with pytest.raises(P.PtkError):
+        FDTDGraph.load(P.reference_params(9, 8, 8), path)
+    with pytest.raises(P.PtkError):
+        FDTDGraph.load(P.reference_params(8, 8, 8), path, "unrolled")
