@@ -279,17 +279,27 @@ public:
 };
 
 // ---------------------------------------------------------------------------------------------
-// A (file, entry) pair resolved to a linked native kernel (CompiledKernel.h).
+// Host-task entry point (hosttask.h:28-31): called with the task's formal parameters as host
+// pointers, in parameter-index order.  (__stdcall has no meaning on the platforms this runs on.)
+typedef void (*LPFNHOSTTASK)(UINT nArguments, void **ppArguments);
+
+// A (file, entry) pair resolved to a linked native kernel, or to a host function exported by a
+// shared library (CompiledKernel.h; hostaccelerator.cpp:328-380 for the host case).
 class CompiledKernel {
 public:
     CompiledKernel(const char *file, const char *entry, int id) : m_file(file), m_entry(entry), m_id(id) {}
+    CompiledKernel(const char *file, const char *entry, LPFNHOSTTASK fn)
+        : m_file(file), m_entry(entry), m_id(-1), m_host(fn) {}
     const char *GetSourceFile() { return m_file.c_str(); }
     const char *GetOperation() { return m_entry.c_str(); }
     int NativeId() const { return m_id; }
+    bool IsHost() const { return m_host != nullptr; }
+    LPFNHOSTTASK HostFunction() const { return m_host; }
 
 private:
     std::string m_file, m_entry;
     int m_id;
+    LPFNHOSTTASK m_host = nullptr;
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -300,7 +310,10 @@ public:
     void SetComputeGeometry(int x = 1, int y = 1, int z = 1);
     void SetBlockAndGridSize(PTASKDIM3 grid, PTASKDIM3 block);
     const char *GetTaskName() { return m_name.c_str(); }
-    ACCELERATOR_CLASS GetAcceleratorClass() { return ACCELERATOR_CLASS_CUDA; }
+    ACCELERATOR_CLASS GetAcceleratorClass()
+    {
+        return m_kernel && m_kernel->IsHost() ? ACCELERATOR_CLASS_HOST : ACCELERATOR_CLASS_CUDA;
+    }
     Graph *GetGraph() { return m_graph; }
     CompiledKernel *GetCompiledKernel() { return m_kernel; }
     UINT GetInputPortCount() { return (UINT)m_inputs.size(); }
@@ -332,6 +345,7 @@ private:
 // ---------------------------------------------------------------------------------------------
 struct GraphStats {
     UINT64 dispatches = 0;         // task dispatches executed one by one
+    UINT64 host_dispatches = 0;    // of which host tasks (entry points of a shared library)
     UINT64 kernel_launches = 0;    // kernels enqueued by dispatches
     UINT64 cycles_lowered = 0;     // iteration loops run as a captured / fused whole
     UINT64 cycle_iterations = 0;   // iterations executed inside lowered loops

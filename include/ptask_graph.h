@@ -44,12 +44,22 @@ typedef struct ptk_graph_stats {
     unsigned long long graph_replays;     /* CUDA-graph launches of lowered loops */
     float last_cycle_ms;                  /* device time of the last lowered loop */
     float last_solve_ms;                  /* host wall time of the last ptk_fdtd_graph_solve */
+    unsigned long long host_dispatches;   /* of the dispatches, host tasks */
 } ptk_graph_stats;
 
 /* Build the FDTD graph for grid p (Graph construction of graphfdtd.cpp:448-739, or its cyclic form)
  * and start it (Graph::Run, ptask/graph.h:216).  `unrolled_steps` is the number of unrolled steps
  * for PTK_GRAPH_UNROLLED and ignored otherwise. */
 int ptk_fdtd_graph_create(const ptk_fdtd_params *p, int mode, int unrolled_steps, ptk_fdtd_graph **out);
+
+/* The unrolled graph with host tasks (hosttask.h:28-31): the tasks of every field whose bit is set
+ * in `host_fields` (bit f = field f, PTK_HX..PTK_EZ) run the entry points HxComputation ..
+ * EzComputation of the shared library `library` ("x.so", or a reference-style "x.dll" name, looked up
+ * as x.dll, x.so and libx.so), called as void f(unsigned n, void **args) with args = (in0, in1, in2,
+ * &FDTD_PARAMS, out) as host pointers; the other fields' tasks run on the GPU.  Blocks move between
+ * host and device as the tasks that read them need.  PTK_ERR_NOTFOUND: library or entry missing. */
+int ptk_fdtd_graph_create_host(const ptk_fdtd_params *p, int unrolled_steps, const char *library,
+                               unsigned host_fields, ptk_fdtd_graph **out);
 
 /* Push the sticky inputs: per-cell coefficients (Nx*Ny*Nz floats each; all NULL = scalar vacuum
  * coefficients Dt/eps0, Dt/mu0 as in the reference) and the soft Ez source (si<0 or wave NULL = none). */

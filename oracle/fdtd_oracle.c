@@ -18,6 +18,8 @@
  *                       Db=fl(Dt/mu0) and the source is off (pinned by tests).
  *   oracle_ext_f64      FP64 twin of oracle_ext_f32 (inputs widened once), for the "error vs FP64"
  *                       figure.
+ *   oracle_field_task_f32  one per-field task (graphfdtd.cpp:185-312), out of place, for the test
+ *                       host-task library.
  *
  * Layouts are the reference's (Simple3DArray.h:33): element (i,j,k) of an array with extents
  * (d1,d2,d3) sits at i + j*d1 + k*d1*d2; the six fields have extents
@@ -232,6 +234,76 @@ int oracle_ext_f64(const float *const in[6], double *const out[6],
                    (double)p->Cy, (double)p->Cz, steps, si, sj, sk, wave, nwave);
     for (q = 0; q < 4; ++q) free(c[q]);
     return rc;
+}
+
+/* One per-field task of the reference graph, out-of-place: field f (0..5 = Hx..Ez) with the inputs
+ * of its task in the reference's port order (graphfdtd.cpp:458-597):
+ *   Hx: (Hx, Ey, Ez)  Hy: (Hy, Ex, Ez)  Hz: (Hz, Ex, Ey)  Ex: (Ex, Hy, Hz)  Ey: (Ey, Hx, Hz)  Ez: (Ez, Hx, Hy)
+ * Restates fdtd_Hx..EzComputation_cpu (graphfdtd.cpp:185-312) with the scalar vacuum coefficients,
+ * the same expressions as step_f32 above (H: 1*H + (Dt/mu0)*curl, E: 1*E + (Dt/eps0)*curl, E faces
+ * copied).  Used by the test host-task library to run the reference graph on the host. */
+int oracle_field_task_f32(int f, const float *a, const float *b, const float *c, const oracle_params *p,
+                          float *out)
+{
+    const int Nx = p->Nx, Ny = p->Ny, Nz = p->Nz;
+    const float Cx = p->Cx, Cy = p->Cy, Cz = p->Cz;
+    const float ch = p->Dt / p->mu0, ce = p->Dt / p->eps0, one = 1.0f;
+    int i, j, k;
+    if (Nx < 1 || Ny < 1 || Nz < 1 || f < 0 || f > 5) return 1;
+    switch (f) {
+    case 0:   /* Hx from Ey, Ez */
+        for (k = 0; k < Nz; ++k) for (j = 0; j < Ny; ++j) for (i = 0; i <= Nx; ++i) {
+            float curl = (b[IDX(i, j, k + 1, Nx + 1, Ny)] - b[IDX(i, j, k, Nx + 1, Ny)]) * Cz
+                       - (c[IDX(i, j + 1, k, Nx + 1, Ny + 1)] - c[IDX(i, j, k, Nx + 1, Ny + 1)]) * Cy;
+            size_t o = IDX(i, j, k, Nx + 1, Ny);
+            out[o] = one * a[o] + ch * curl;
+        }
+        break;
+    case 1:   /* Hy from Ex, Ez */
+        for (k = 0; k < Nz; ++k) for (j = 0; j <= Ny; ++j) for (i = 0; i < Nx; ++i) {
+            float curl = (c[IDX(i + 1, j, k, Nx + 1, Ny + 1)] - c[IDX(i, j, k, Nx + 1, Ny + 1)]) * Cx
+                       - (b[IDX(i, j, k + 1, Nx, Ny + 1)] - b[IDX(i, j, k, Nx, Ny + 1)]) * Cz;
+            size_t o = IDX(i, j, k, Nx, Ny + 1);
+            out[o] = one * a[o] + ch * curl;
+        }
+        break;
+    case 2:   /* Hz from Ex, Ey */
+        for (k = 0; k <= Nz; ++k) for (j = 0; j < Ny; ++j) for (i = 0; i < Nx; ++i) {
+            float curl = (b[IDX(i, j + 1, k, Nx, Ny + 1)] - b[IDX(i, j, k, Nx, Ny + 1)]) * Cy
+                       - (c[IDX(i + 1, j, k, Nx + 1, Ny)] - c[IDX(i, j, k, Nx + 1, Ny)]) * Cx;
+            size_t o = IDX(i, j, k, Nx, Ny);
+            out[o] = one * a[o] + ch * curl;
+        }
+        break;
+    case 3:   /* Ex from Hy, Hz */
+        for (k = 0; k <= Nz; ++k) for (j = 0; j <= Ny; ++j) for (i = 0; i < Nx; ++i) {
+            size_t o = IDX(i, j, k, Nx, Ny + 1);
+            if (j < 1 || k < 1 || j > Ny - 1 || k > Nz - 1) { out[o] = a[o]; continue; }
+            float curl = (c[IDX(i, j, k, Nx, Ny)] - c[IDX(i, j - 1, k, Nx, Ny)]) * Cy
+                       - (b[IDX(i, j, k, Nx, Ny + 1)] - b[IDX(i, j, k - 1, Nx, Ny + 1)]) * Cz;
+            out[o] = one * a[o] + ce * curl;
+        }
+        break;
+    case 4:   /* Ey from Hx, Hz */
+        for (k = 0; k <= Nz; ++k) for (j = 0; j < Ny; ++j) for (i = 0; i <= Nx; ++i) {
+            size_t o = IDX(i, j, k, Nx + 1, Ny);
+            if (i < 1 || k < 1 || i > Nx - 1 || k > Nz - 1) { out[o] = a[o]; continue; }
+            float curl = (b[IDX(i, j, k, Nx + 1, Ny)] - b[IDX(i, j, k - 1, Nx + 1, Ny)]) * Cz
+                       - (c[IDX(i, j, k, Nx, Ny)] - c[IDX(i - 1, j, k, Nx, Ny)]) * Cx;
+            out[o] = one * a[o] + ce * curl;
+        }
+        break;
+    default:  /* Ez from Hx, Hy */
+        for (k = 0; k < Nz; ++k) for (j = 0; j <= Ny; ++j) for (i = 0; i <= Nx; ++i) {
+            size_t o = IDX(i, j, k, Nx + 1, Ny + 1);
+            if (i < 1 || j < 1 || i > Nx - 1 || j > Ny - 1) { out[o] = a[o]; continue; }
+            float curl = (c[IDX(i, j, k, Nx, Ny + 1)] - c[IDX(i - 1, j, k, Nx, Ny + 1)]) * Cx
+                       - (b[IDX(i, j, k, Nx + 1, Ny)] - b[IDX(i, j - 1, k, Nx + 1, Ny)]) * Cy;
+            out[o] = one * a[o] + ce * curl;
+        }
+        break;
+    }
+    return 0;
 }
 
 /* Threads the OpenMP runtime will use (1 when built without OpenMP). */

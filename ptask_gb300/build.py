@@ -111,7 +111,7 @@ def build_runtime(verbose: bool = False) -> Path | None:
     core = BUILD / "libptask_gb300.so"
     if jobs or _newer(lib, objs + [core]):
         _run(["g++", "-shared", "-o", str(lib)] + [str(o) for o in objs] +
-             ["-L", str(BUILD), "-lptask_gb300", "-pthread", "-Wl,-rpath,$ORIGIN"])
+             ["-L", str(BUILD), "-lptask_gb300", "-pthread", "-ldl", "-Wl,-rpath,$ORIGIN"])
     bindir = BUILD / "bin"
     bindir.mkdir(exist_ok=True)
     jobs = []

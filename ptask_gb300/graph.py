@@ -18,7 +18,8 @@ MODES = {"fused": CYCLIC_FUSED, "captured": CYCLIC_CAPTURED, "taskwise": CYCLIC_
 class GraphStats(C.Structure):
     _fields_ = [("dispatches", C.c_ulonglong), ("kernel_launches", C.c_ulonglong),
                 ("cycles_lowered", C.c_ulonglong), ("cycle_iterations", C.c_ulonglong),
-                ("graph_replays", C.c_ulonglong), ("last_cycle_ms", C.c_float), ("last_solve_ms", C.c_float)]
+                ("graph_replays", C.c_ulonglong), ("last_cycle_ms", C.c_float), ("last_solve_ms", C.c_float),
+                ("host_dispatches", C.c_ulonglong)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -35,6 +36,7 @@ _SIGS = {
     "ptk_fdtd_graph_write_dot": [_P, C.c_char_p],
     "ptk_fdtd_graph_destroy": [_P],
     "ptk_fdtd_graph_save": [_P, C.c_char_p],
+    "ptk_fdtd_graph_create_host": [C.POINTER(FdtdParams), C.c_int, C.c_char_p, C.c_uint, C.POINTER(_P)],
     "ptk_fdtd_graph_load": [C.POINTER(FdtdParams), C.c_int, C.c_char_p, C.POINTER(_P)],
     "ptk_fdtd_graph_export": [C.POINTER(FdtdParams), C.c_int, C.c_int, C.c_char_p],
     "ptk_graph_xml_roundtrip": [C.c_char_p, C.c_char_p],
@@ -72,6 +74,15 @@ class FDTDGraph:
             return
         _check(rt().ptk_fdtd_graph_create(C.byref(params), MODES[mode], unrolled_steps, C.byref(self._h)),
                "ptk_fdtd_graph_create")
+
+    @classmethod
+    def with_host_tasks(cls, params: FdtdParams, steps: int, library, host_fields: int = 0x3F) -> "FDTDGraph":
+        """The unrolled graph whose tasks for the fields in `host_fields` (bit f = field f) are host
+        tasks from the shared library `library` (entry points HxComputation .. EzComputation)."""
+        h = C.c_void_p()
+        _check(rt().ptk_fdtd_graph_create_host(C.byref(params), steps, str(library).encode(), host_fields,
+                                               C.byref(h)), "ptk_fdtd_graph_create_host")
+        return cls(params, "unrolled", _handle=h)
 
     @classmethod
     def load(cls, params: FdtdParams, path, mode: str = "fused") -> "FDTDGraph":

@@ -52,6 +52,8 @@ struct ptk_fdtd_graph {
     bool problem_set = false;
     float last_solve_ms = 0;
     UINT uid = 0;
+    std::string host_library;   // unrolled graph: tasks of the fields in host_fields are host tasks
+    unsigned host_fields = 0;
 };
 
 namespace {
@@ -60,7 +62,9 @@ namespace {
 Task *field_task(ptk_fdtd_graph *G, const char *kernel, const char *task, int out_field, const int in_fields[3],
                  Port **in, Port **out)
 {
-    CompiledKernel *k = Runtime::GetCompiledKernel("fdtdMain.compute_10.ptx", kernel);
+    const bool host = (G->host_fields >> out_field) & 1u;
+    CompiledKernel *k = Runtime::GetCompiledKernel(host ? G->host_library.c_str() : "fdtdMain.compute_10.ptx", kernel);
+    if (!k) return nullptr;
     for (int q = 0; q < 3; ++q)
         in[q] = Runtime::CreatePort(INPUT_PORT, G->field_t[in_fields[q]], G->uid++, kFieldNames[in_fields[q]], q);
     in[3] = Runtime::CreatePort(STICKY_PORT, G->param_t, G->uid++, "Config", 3);
@@ -68,11 +72,14 @@ Task *field_task(ptk_fdtd_graph *G, const char *kernel, const char *task, int ou
     Task *t = G->g->AddTask(k, 4, in, 1, out, task);
     UINT e[3];
     extents(out_field, G->p.Nx, G->p.Ny, G->p.Nz, e);
-    t->SetComputeGeometry((int)e[0], (int)e[1], (int)e[2]);
+    // A host task's geometry is the number of times its entry point runs (hosttask.cpp:330-338):
+    // once, since the entry point updates the whole field.
+    if (host) t->SetComputeGeometry(1, 1, 1);
+    else t->SetComputeGeometry((int)e[0], (int)e[1], (int)e[2]);
     return t;
 }
 
-void build_unrolled(ptk_fdtd_graph *G, int steps)
+bool build_unrolled(ptk_fdtd_graph *G, int steps)
 {
     static const char *kernels[6] = {"HxComputation", "HyComputation", "HzComputation",
                                      "ExComputation", "EyComputation", "EzComputation"};
@@ -83,7 +90,7 @@ void build_unrolled(ptk_fdtd_graph *G, int steps)
         Port *in[6][4], *out[6][1];
         for (int f = 0; f < 6; ++f) {
             std::string name = std::string(kFieldNames[f]) + "ComTask_" + std::to_string(s);
-            field_task(G, kernels[f], name.c_str(), f, ins[f], in[f], out[f]);
+            if (!field_task(G, kernels[f], name.c_str(), f, ins[f], in[f], out[f])) return false;
             G->param_in.push_back(G->g->AddInputChannel(in[f][3], ("ConstParam" + name).c_str()));
         }
         // H outputs feed the E tasks of the same step (graphfdtd.cpp:606-615)
@@ -111,6 +118,7 @@ void build_unrolled(ptk_fdtd_graph *G, int steps)
             }
     }
     for (GraphInputChannel *c : G->param_in) c->SetNoDraw();
+    return true;
 }
 
 // ---- cyclic graph -----------------------------------------------------------------------------
@@ -302,6 +310,26 @@ int ptk_fdtd_graph_create(const ptk_fdtd_params *p, int mode, int unrolled_steps
     return PTK_OK;
 }
 
+int ptk_fdtd_graph_create_host(const ptk_fdtd_params *p, int unrolled_steps, const char *library,
+                               unsigned host_fields, ptk_fdtd_graph **out)
+{
+    if (!p || !out || !library || p->Nx < 1 || p->Ny < 1 || p->Nz < 1 || unrolled_steps < 1 || host_fields > 0x3Fu)
+        return PTK_ERR_INVALID;
+    Runtime::SetExitOnRuntimeFailure(FALSE);
+    if (PTFAILED(Runtime::Initialize())) return PTK_ERR_CUDA;
+    ptk_fdtd_graph *G = new_graph(p, PTK_GRAPH_UNROLLED, unrolled_steps);
+    G->host_library = library;
+    G->host_fields = host_fields;
+    if (!build_unrolled(G, unrolled_steps)) {
+        Graph::DestroyGraph(G->g);
+        delete G;
+        return PTK_ERR_NOTFOUND;
+    }
+    start(G);
+    *out = G;
+    return PTK_OK;
+}
+
 int ptk_fdtd_graph_export(const ptk_fdtd_params *p, int mode, int unrolled_steps, const char *path)
 {
     if (!p || !path || p->Nx < 1 || p->Ny < 1 || p->Nz < 1 || mode < 0 || mode > 3) return PTK_ERR_INVALID;
@@ -454,6 +482,7 @@ int ptk_fdtd_graph_stats(const ptk_fdtd_graph *G, ptk_graph_stats *st)
     if (!G || !st) return PTK_ERR_INVALID;
     GraphStats s = G->g->GetStats();
     st->dispatches = s.dispatches;
+    st->host_dispatches = s.host_dispatches;
     st->kernel_launches = s.kernel_launches;
     st->cycles_lowered = s.cycles_lowered;
     st->cycle_iterations = s.cycle_iterations;

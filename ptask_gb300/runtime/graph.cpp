@@ -478,6 +478,8 @@ void Graph::finalize()
                         top = d;
                     }
             if (!ok || !top) continue;
+            // host tasks run where they are: only loops of native kernels are lowered to the GPU
+            if (top->GetCompiledKernel()->IsHost() || b->GetCompiledKernel()->IsHost()) continue;
             auto plan = std::make_unique<CyclePlan>();
             plan->top = top;
             plan->bottom = b;
@@ -720,7 +722,9 @@ void Graph::dispatch(Task *t)
             owned.push_back(out[r]);
         }
 
-    // Formal parameters in index order.
+    // Formal parameters in index order: device views for a native kernel, host views for a host
+    // task (whose writes leave the host copy as the only valid one).
+    const bool host = t->GetCompiledKernel()->IsHost();
     std::vector<std::pair<int, Formal>> formals;
     for (size_t q = 0; q < t->m_inputs.size(); ++q) {
         Port *p = t->m_inputs[q];
@@ -728,6 +732,7 @@ void Graph::dispatch(Task *t)
         Formal f{p, in[q], nullptr, nullptr};
         if (in[q]) {
             if (is_scalar(in[q])) f.host = in[q]->HostBytes();
+            else if (host) f.host = in[q]->GetDataPointer(p->IsInOutParameter(), TRUE);
             else f.dev = in[q]->DeviceView(m_stream, p->IsInOutParameter(), true);
         }
         formals.push_back({(int)p->GetFormalParameterIndex(), f});
@@ -735,7 +740,9 @@ void Graph::dispatch(Task *t)
     for (size_t r = 0; r < t->m_outputs.size(); ++r) {
         Port *p = t->m_outputs[r];
         if (p->GetFormalParameterIndex() == (UINT)-1) continue;
-        Formal f{p, out[r], out[r]->DeviceView(m_stream, true, false), nullptr};
+        Formal f{p, out[r], nullptr, nullptr};
+        if (host) f.host = out[r]->GetDataPointer(TRUE, FALSE);
+        else f.dev = out[r]->DeviceView(m_stream, true, false);
         formals.push_back({(int)p->GetFormalParameterIndex(), f});
     }
     std::stable_sort(formals.begin(), formals.end(),
@@ -743,23 +750,43 @@ void Graph::dispatch(Task *t)
     std::vector<Formal> fv;
     for (auto &pf : formals) fv.push_back(pf.second);
 
-    for (UINT n = 0; n < repeat; ++n) {
-        int rc = launch_native(t, fv, m_stream);
-        if (rc != PTK_OK) {
-            Runtime::HandleError("dispatch of task %s (%s) failed: %s", t->GetTaskName(),
-                                 t->GetCompiledKernel()->GetOperation(), ptk_last_error());
-            break;
+    if (host) {
+        // Host task (hosttask.cpp:305-340): the arguments are the formal parameters 0..n-1 as host
+        // pointers; the entry point runs once per point of the task's geometry.
+        std::vector<void *> args;
+        for (size_t i = 0; i < formals.size(); ++i) {
+            if (formals[i].first != (int)i) {
+                Runtime::HandleError("dispatch of host task %s: no formal parameter %zu", t->GetTaskName(), i);
+                args.clear();
+                break;
+            }
+            args.push_back(const_cast<void *>(formals[i].second.host));
         }
-        ++m_stats.kernel_launches;
+        const UINT reps = repeat * std::max(1, t->m_geom.x) * std::max(1, t->m_geom.y) * std::max(1, t->m_geom.z);
+        if (args.size() == formals.size())
+            for (UINT n = 0; n < reps; ++n) t->GetCompiledKernel()->HostFunction()((UINT)args.size(), args.data());
+        ++m_stats.host_dispatches;
+    } else {
+        for (UINT n = 0; n < repeat; ++n) {
+            int rc = launch_native(t, fv, m_stream);
+            if (rc != PTK_OK) {
+                Runtime::HandleError("dispatch of task %s (%s) failed: %s", t->GetTaskName(),
+                                     t->GetCompiledKernel()->GetOperation(), ptk_last_error());
+                break;
+            }
+            ++m_stats.kernel_launches;
+        }
     }
     ++t->m_dispatches;
     ++m_stats.dispatches;
 
-    // Written blocks get a completion event.
-    for (size_t q = 0; q < t->m_inputs.size(); ++q)
-        if (t->m_inputs[q]->IsInOutParameter() && in[q] && !is_scalar(in[q])) in[q]->DeviceWritten(m_stream);
-    for (size_t r = 0; r < out.size(); ++r)
-        if (t->m_outputs[r]->GetFormalParameterIndex() != (UINT)-1) out[r]->DeviceWritten(m_stream);
+    // Blocks a kernel wrote get a completion event (a host task's writes are already complete).
+    if (!host) {
+        for (size_t q = 0; q < t->m_inputs.size(); ++q)
+            if (t->m_inputs[q]->IsInOutParameter() && in[q] && !is_scalar(in[q])) in[q]->DeviceWritten(m_stream);
+        for (size_t r = 0; r < out.size(); ++r)
+            if (t->m_outputs[r]->GetFormalParameterIndex() != (UINT)-1) out[r]->DeviceWritten(m_stream);
+    }
 
     // Control propagation of the general iterator.
     if (general && meta) {

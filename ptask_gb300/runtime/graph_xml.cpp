@@ -558,8 +558,11 @@ void Graph::Deserialize(const char *filename)
             const std::string name = str_of(*t, "Name");
             auto ki = kmap.find(int_of(*t, "KernelID"));
             if (ki == kmap.end()) throw LoadError{"task " + name + ": unknown KernelID"};
-            if (int_of(*t, "AcceleratorClass") != (int)ACCELERATOR_CLASS_CUDA)
-                throw LoadError{"task " + name + ": only CUDA tasks run on this runtime"};
+            const long long cls = int_of(*t, "AcceleratorClass");
+            const long long have = ki->second->IsHost() ? (long long)ACCELERATOR_CLASS_HOST : (long long)ACCELERATOR_CLASS_CUDA;
+            if (cls != have)
+                throw LoadError{"task " + name + ": accelerator class " + std::to_string(cls) + " but its kernel is " +
+                                (ki->second->IsHost() ? "a host task" : "a CUDA kernel")};
             std::vector<Port *> ins, outs;
             read_ports(need(*t, "InputPorts"), ins);
             read_ports(need(*t, "OutputPorts"), outs);

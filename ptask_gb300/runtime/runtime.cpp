@@ -1,5 +1,7 @@
 // runtime.cpp -- PTask::Runtime entry points, datablock templates, datablocks and kernel
 // resolution for the GB300 runtime.  Device work goes through the C ABI of libptask_gb300.so.
+#include <dlfcn.h>
+
 #include <cstdarg>
 #include <cstdlib>
 #include <map>
@@ -13,7 +15,7 @@ namespace PTask {
 namespace {
 
 struct Config {
-    BOOL use_cuda = TRUE, use_opencl = FALSE, use_dx = FALSE, use_host = FALSE;
+    BOOL use_cuda = TRUE, use_opencl = FALSE, use_dx = FALSE, use_host = TRUE;   // PTaskRuntime.cpp:2298
     BOOL verbose = FALSE;
     int channel_capacity = 4;             // DEFAULT_CHANNEL_CAPACITY, PTaskRuntime.cpp:79
     SCHEDULINGMODE sched = SCHEDMODE_DATADRIVEN;
@@ -377,12 +379,55 @@ Datablock *AllocateDatablock(DatablockTemplate *t, void *init, UINT cb, BUFFERAC
     return AllocateDatablock(t, init, cb, nullptr, flags, ctl);
 }
 
+// A kernel file that names a shared library holds host tasks: "x.so", or the reference's "x.dll",
+// which is looked up as x.dll, x.so and libx.so in the same directory.
+static bool is_host_library(const std::string &f)
+{
+    auto ends = [&](const char *e) { return f.size() >= strlen(e) && f.compare(f.size() - strlen(e), strlen(e), e) == 0; };
+    return ends(".dll") || ends(".so") || f.find(".so.") != std::string::npos;
+}
+
+static void *open_host_library(const std::string &f, std::string &why)
+{
+    std::vector<std::string> names{f};
+    if (f.size() > 4 && f.compare(f.size() - 4, 4, ".dll") == 0) {
+        const size_t slash = f.find_last_of('/');
+        const std::string dir = slash == std::string::npos ? "" : f.substr(0, slash + 1);
+        const std::string stem = f.substr(dir.size(), f.size() - dir.size() - 4);
+        names.push_back(dir + stem + ".so");
+        names.push_back(dir + "lib" + stem + ".so");
+    }
+    for (const std::string &n : names) {
+        // a bare name would make dlopen search the system paths: look in the current directory
+        const std::string path = n.find('/') == std::string::npos ? "./" + n : n;
+        if (void *h = dlopen(path.c_str(), RTLD_NOW | RTLD_LOCAL)) return h;
+        const char *e = dlerror();
+        why = e ? e : "dlopen failed";
+    }
+    return nullptr;
+}
+
 CompiledKernel *GetCompiledKernel(const char *file, const char *op, char *out, int outsz, int, int, int)
 {
     std::lock_guard<std::mutex> lk(g_mu);
     std::string key = std::string(file ? file : "") + "|" + (op ? op : "");
     auto it = g_kernels.find(key);
     if (it != g_kernels.end()) return it->second;
+    if (file && op && is_host_library(file)) {
+        // Host task: the entry point of a shared library (hostaccelerator.cpp:328-380).
+        std::string why = "host tasks are disabled (SetUseHost)";
+        void *h = g_cfg.use_host ? open_host_library(file, why) : nullptr;
+        void *fn = h ? dlsym(h, op) : nullptr;
+        if (h && !fn) why = std::string("no entry point ") + op + " in " + file;
+        if (!fn) {
+            if (out && outsz > 0) snprintf(out, (size_t)outsz, "%s", why.c_str());
+            return nullptr;
+        }
+        auto *k = new CompiledKernel(file, op, reinterpret_cast<LPFNHOSTTASK>(fn));
+        g_kernels[key] = k;
+        if (out && outsz > 0) out[0] = 0;
+        return k;
+    }
     int id = -1;
     if (ptk_kernel_lookup(file, op, &id) != PTK_OK) {
         if (out && outsz > 0) snprintf(out, (size_t)outsz, "%s", ptk_last_error());
@@ -396,6 +441,7 @@ CompiledKernel *GetCompiledKernel(const char *file, const char *op, char *out, i
 
 BOOL CanExecuteKernel(const char *file)
 {
+    if (file && is_host_library(file)) return g_cfg.use_host;   // the host accelerator always exists
     return (g_cfg.use_cuda && ptk_can_execute_kernel(file)) ? TRUE : FALSE;
 }
 

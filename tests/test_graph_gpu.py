@@ -153,3 +153,67 @@ def test_load_rejects_a_file_for_another_grid(tmp_path):
         FDTDGraph.load(P.reference_params(9, 8, 8), path)
     with pytest.raises(P.PtkError):
         FDTDGraph.load(P.reference_params(8, 8, 8), path, "unrolled")
+
+
+# ------------------------------------------------------------------------------------------------
+# Host tasks (hosttask.h:28-31): the same graph with its tasks on the host, on the GPU, or mixed.
+# ------------------------------------------------------------------------------------------------
+@pytest.fixture(scope="module")
+def host_library(tmp_path_factory):
+    """tests/hosttasks/fdtd_hosttasks.c built against the oracle into a shared library."""
+    import subprocess
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    odir = root / "oracle" / "_build"
+    out = tmp_path_factory.mktemp("hosttasks") / "libfdtd_hosttasks.so"
+    subprocess.run(["gcc", "-O2", "-shared", "-fPIC", "-ffp-contract=off",
+                    str(root / "tests" / "hosttasks" / "fdtd_hosttasks.c"), "-L", str(odir), "-loracle",
+                    "-Wl,-rpath," + str(odir), "-o", str(out)], check=True)
+    return out
+
+
+@pytest.mark.parametrize("host_fields", [0x3F, 0x07, 0x38, 0x15])
+def test_host_task_graph_matches_gpu_graph(host_library, host_fields):
+    shape, steps = (20, 14, 6), 3
+    p = P.reference_params(*shape)
+    f = P.random_fields(*shape, seed=64)
+    with FDTDGraph.with_host_tasks(p, steps, host_library, host_fields) as g:
+        got = g.solve(f, steps)
+        st = g.stats()
+    n_host = bin(host_fields).count("1")
+    assert st["host_dispatches"] == n_host * steps and st["dispatches"] == 6 * steps
+    assert st["kernel_launches"] == (6 - n_host) * steps
+    assert_same(got, oracle.step_ref_f32(f, steps, p), f"host fields {host_fields:#x}")
+
+
+def test_host_tasks_by_reference_dll_name(host_library):
+    """The reference names host libraries "x.dll": looked up as libx.so beside it."""
+    shape, steps = (9, 7, 5), 2
+    p = P.reference_params(*shape)
+    f = P.random_fields(*shape, seed=65)
+    dll = host_library.parent / "fdtd_hosttasks.dll"
+    with FDTDGraph.with_host_tasks(p, steps, dll, 0x3F) as g:
+        got = g.solve(f, steps)
+    assert_same(got, oracle.step_ref_f32(f, steps, p), "dll name")
+
+
+def test_host_task_graph_file_roundtrip(host_library, tmp_path):
+    shape, steps = (12, 10, 4), 2
+    p = P.reference_params(*shape)
+    f = P.random_fields(*shape, seed=66)
+    path = tmp_path / "host.xml"
+    with FDTDGraph.with_host_tasks(p, steps, host_library, 0x07) as g:
+        g.save(path)
+    assert path.read_text().count("<AcceleratorClass>4</AcceleratorClass>") == 3 * steps   # HOST
+    with FDTDGraph.load(p, path) as g:
+        got = g.solve(f, steps)
+        assert g.stats()["host_dispatches"] == 3 * steps
+    assert_same(got, oracle.step_ref_f32(f, steps, p), "loaded host graph")
+
+
+def test_missing_host_library_or_entry(tmp_path, host_library):
+    p = P.reference_params(8, 8, 4)
+    with pytest.raises(P.PtkError):
+        FDTDGraph.with_host_tasks(p, 1, tmp_path / "absent.so", 0x3F)
+    with pytest.raises(P.PtkError):
+        FDTDGraph.with_host_tasks(p, 1, host_library.parent / "libm_absent.so", 0x01)
