@@ -162,9 +162,9 @@ typedef struct ptk_solver ptk_solver;
 
 /* Tile shape of the fused step kernel.  by: rows per CTA (4, 8 or 16); kc: z-planes per CTA (>=1,
  * 0 = whole depth); vec: x cells per thread (1, 2 or 4; tiles are 32*vec cells wide, 0 = choose
- * from Nx); stages: 0 = operands loaded into registers, 2..5 = operands staged into shared memory
- * by TMA tensor copies with that many z-planes in the ring (needs vec 4 and by 4 or 8; by 8 up to
- * 4 stages).
+ * from Nx); stages: 0 = operands loaded into registers, 2..6 = operands staged into shared memory
+ * by TMA tensor copies with that many z-planes in the ring (needs vec 4 and by 4 or 8; 5 and 6
+ * stages only with the material index, see ptk_solver_use_material_index).
  * by = kc = 0 selects the default shape. */
 typedef struct ptk_tile_config {
     int by;
@@ -190,6 +190,16 @@ int ptk_solver_set_source(ptk_solver *s, int i, int j, int k, const float *wave,
 int ptk_solver_reset_clock(ptk_solver *s, void *stream);
 /* Tile shape for subsequent runs (see ptk_tile_config). */
 int ptk_solver_set_tiles(ptk_solver *s, const ptk_tile_config *cfg);
+/* Coefficients with few distinct (Ca, Cb, Da, Db) tuples (at most 256, the usual case: a handful of
+ * materials) are also kept as a one-byte material index per node plus a table; the staged kernel
+ * then reads 49 bytes per cell update instead of 64, with identical results.  On by default;
+ * `enable` = 0 keeps the per-cell arrays only.  The index is rebuilt whenever coefficients are set. */
+int ptk_solver_use_material_index(ptk_solver *s, int enable, void *stream);
+/* Materials in the current index (0: none, the per-cell arrays are read). */
+int ptk_solver_material_count(const ptk_solver *s, int *nmat);
+/* The step kernel the next run uses: ring stages (0 = register kernel) and whether it reads the
+ * material index.  A staged shape with no per-cell-array instantiation falls back to 4 stages. */
+int ptk_solver_kernel(const ptk_solver *s, int *stages, int *material_index);
 int ptk_solver_get_tiles(const ptk_solver *s, ptk_tile_config *cfg);
 /* Advance `steps` time steps, asynchronously on `stream`. */
 int ptk_solver_run(ptk_solver *s, int steps, void *stream);

@@ -118,6 +118,9 @@ _SIGS = {
     "ptk_solver_reset_clock": (C.c_int, [_P, _P]),
     "ptk_solver_set_tiles": (C.c_int, [_P, C.POINTER(TileConfig)]),
     "ptk_solver_get_tiles": (C.c_int, [_P, C.POINTER(TileConfig)]),
+    "ptk_solver_use_material_index": (C.c_int, [_P, C.c_int, _P]),
+    "ptk_solver_material_count": (C.c_int, [_P, C.POINTER(C.c_int)]),
+    "ptk_solver_kernel": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "ptk_solver_run": (C.c_int, [_P, C.c_int, _P]),
     "ptk_solver_get_fields": (C.c_int, [_P, C.POINTER(_P), C.c_int, _P]),
     "ptk_solver_bytes": (C.c_int, [_P, C.POINTER(C.c_size_t)]),

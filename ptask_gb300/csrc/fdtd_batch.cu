@@ -35,19 +35,23 @@ struct BoxArgs {
 };
 
 // Padded coefficients of a generated problem: the device twin of ptk_problem_generate (same boxes,
-// same FP32 expressions Cb = Dt/(eps0*eps_r), Db = Dt/mu0; wall nodes take the nearest cell).
+// same FP32 expressions Cb = Dt/(eps0*eps_r), Db = Dt/mu0; wall nodes take the nearest cell).  With
+// `mat`, also the material index: 0 for vacuum, b + 1 inside box b (the last box listed wins).
 __global__ void k_generate_coefs(BoxArgs boxes, int nx, int ny, int nz, int pitch, long long plane, float dt,
-                                 float eps0, float mu0, float *Ca, float *Cb, float *Da, float *Db)
+                                 float eps0, float mu0, float *Ca, float *Cb, float *Da, float *Db,
+                                 unsigned char *mat)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y, k = blockIdx.z;
     if (i > nx) return;
     const int ci = min(i, nx - 1), cj = min(j, ny - 1), ck = min(k, nz - 1);
     float e = 1.0f;
+    int id = 0;
     for (int b = boxes.n - 1; b >= 0; --b)
         if (ci >= boxes.lo[b][0] && ci < boxes.hi[b][0] && cj >= boxes.lo[b][1] && cj < boxes.hi[b][1] &&
             ck >= boxes.lo[b][2] && ck < boxes.hi[b][2]) {
             e = boxes.epsr[b];
+            id = b + 1;
             break;
         }
     const long long o = i + (long long)pitch * j + plane * k;
@@ -55,6 +59,17 @@ __global__ void k_generate_coefs(BoxArgs boxes, int nx, int ny, int nz, int pitc
     Cb[o] = __fdiv_rn(dt, __fmul_rn(eps0, e));
     Da[o] = 1.0f;
     Db[o] = __fdiv_rn(dt, mu0);
+    if (mat) mat[o] = (unsigned char)id;
+}
+
+// The material table of a generated problem: entry 0 vacuum, entry b + 1 box b, with the
+// coefficient expressions of k_generate_coefs.
+__global__ void k_generate_table(BoxArgs boxes, float dt, float eps0, float mu0, float4 *tab)
+{
+    const int t = threadIdx.x;
+    if (t > boxes.n) return;
+    const float e = t == 0 ? 1.0f : boxes.epsr[t - 1];
+    tab[t] = make_float4(1.0f, __fdiv_rn(dt, __fmul_rn(eps0, e)), 1.0f, __fdiv_rn(dt, mu0));
 }
 
 // Sum of each valid field element (FP64; order of accumulation not fixed, for reporting only).
@@ -77,6 +92,9 @@ struct Inst {
     float *coef[4] = {};
     float *wave = nullptr;
     void *tma = nullptr;        // tensor maps of the staged kernel
+    unsigned char *mat = nullptr;   // material index (staged kernel)
+    float *mat_tab = nullptr;
+    int nmat = 0;
     int nwave = 0;
     long long src = -1;
     int steps_total = 0, done = 0;
@@ -91,8 +109,8 @@ struct Inst {
 
 size_t instance_bytes(const Layout &L, int nwave)
 {
-    return (size_t)L.total * sizeof(float) * 16 + (size_t)nwave * sizeof(float) + 6 * sizeof(double) + kTmaSetBytes +
-           4096;
+    return (size_t)L.total * (sizeof(float) * 16 + 1) + (size_t)nwave * sizeof(float) + 6 * sizeof(double) +
+           kTmaSetBytes + (size_t)kMaxMaterials * 4 * sizeof(float) + 4096;
 }
 
 }  // namespace ptk
@@ -208,6 +226,11 @@ InstDesc instance_desc(const ptk_server *s, const Inst *in)
     d.step = in->done;
     d.steps_left = in->steps_total - in->done;
     d.tma = in->tma;
+    if (s->stages) {
+        d.mat = in->mat;
+        d.mat_tab = in->mat_tab;
+        d.nmat = in->nmat;
+    }
     plan_tiles(d, s->rows, instance_depth(s, in->L.nz), s->vec);
     return d;
 }
@@ -229,11 +252,14 @@ int admit(ptk_server *s, Inst *in)
     for (int c = 0; c < 4 && !rc; ++c) rc = pool_alloc(bytes, st, (void **)&in->coef[c]);
     if (!rc) rc = pool_alloc(6 * sizeof(double), st, (void **)&in->d_sum);
     if (!rc && s->stages) rc = pool_alloc(kTmaSetBytes, st, &in->tma);
+    if (!rc && s->stages) rc = pool_alloc((size_t)in->L.total, st, (void **)&in->mat);
+    if (!rc && s->stages) rc = pool_alloc((size_t)kMaxMaterials * 4 * sizeof(float), st, (void **)&in->mat_tab);
     in->nwave = (si >= 0 && !wave.empty()) ? (int)wave.size() : 0;
     if (!rc && in->nwave) rc = pool_alloc(wave.size() * sizeof(float), st, (void **)&in->wave);
     if (rc) return rc;
     for (int b = 0; b < 2; ++b)
         for (int f = 0; f < 6; ++f) PTK_CUDA_TRY(cudaMemsetAsync(in->buf[b][f], 0, bytes, st));
+    if (in->mat) PTK_CUDA_TRY(cudaMemsetAsync(in->mat, 0, (size_t)in->L.total, st));
     BoxArgs ba{};
     ba.n = (int)boxes.size();
     for (int b = 0; b < ba.n; ++b) {
@@ -245,9 +271,16 @@ int admit(ptk_server *s, Inst *in)
     }
     dim3 grid((in->L.nx + 1 + 127) / 128, in->L.ny + 1, in->L.nz + 1);
     k_generate_coefs<<<grid, 128, 0, st>>>(ba, in->L.nx, in->L.ny, in->L.nz, in->L.pitch, in->L.plane, in->p.Dt,
-                                           in->p.eps0, in->p.mu0, in->coef[0], in->coef[1], in->coef[2], in->coef[3]);
+                                           in->p.eps0, in->p.mu0, in->coef[0], in->coef[1], in->coef[2], in->coef[3],
+                                           in->mat);
     PTK_CUDA_TRY(cudaGetLastError());
     count_launches(1);
+    if (in->mat) {
+        k_generate_table<<<1, 128, 0, st>>>(ba, in->p.Dt, in->p.eps0, in->p.mu0, reinterpret_cast<float4 *>(in->mat_tab));
+        PTK_CUDA_TRY(cudaGetLastError());
+        count_launches(1);
+        in->nmat = ba.n + 1;
+    }
     if (in->nwave) {
         // pageable source: the copy is staged before this returns, so `wave` may go out of scope
         PTK_CUDA_TRY(cudaMemcpyAsync(in->wave, wave.data(), wave.size() * sizeof(float), cudaMemcpyHostToDevice, st));
@@ -278,6 +311,10 @@ void release(ptk_server *s, Inst *in)
     pool_free(in->d_sum, s->st);
     pool_free(in->tma, s->st);
     in->tma = nullptr;
+    pool_free(in->mat, s->st);
+    pool_free(in->mat_tab, s->st);
+    in->mat = nullptr;
+    in->mat_tab = nullptr;
     for (int b = 0; b < 2; ++b)
         for (int f = 0; f < 6; ++f) in->buf[b][f] = nullptr;
     s->used -= in->bytes;
@@ -337,7 +374,7 @@ int chunk_graph(ptk_server *s, int len, int grid, cudaGraphExec_t *out)
         count_launches(1);
     for (int q = 0; q < len && !rc; ++q)
         rc = s->stages ? launch_yee_step_bulk(s->d_desc, s->d_tile0, n, s->total_tiles, q, s->rows, s->stages, grid,
-                                              s->d_err, cap, s->d_work)
+                                              s->d_err, cap, s->d_work, true)
                        : launch_yee_step_v(s->d_desc, s->d_tile0, n, s->total_tiles, q, s->rows, s->vec, grid, cap);
     if (!rc) rc = launch_advance(s->d_desc, n, len, cap);
     set_capturing(false);
@@ -412,7 +449,7 @@ int ptk_server_create(const ptk_server_config *cfg, ptk_server **out)
         s->stages = s->rows == 4 ? 3 : 4;
     } else {
         s->stages = s->cfg.stages;
-        if (yee_bulk_smem_bytes(s->rows, s->stages) == 0) {
+        if (yee_bulk_smem_bytes(s->rows, s->stages, true) == 0) {
             delete s;
             return set_error(PTK_ERR_INVALID, "no staged kernel for %d rows with %d stages", cfg->tile_rows,
                              cfg->stages);
@@ -478,7 +515,8 @@ int ptk_server_run(ptk_server *s, double time_scale)
     size_t nxt = 0;
     int grid_cap[5] = {0, 0, 0, 0, 0};   // resident CTAs per vec (1, 2, 4)
     for (int v : {1, 2, 4})
-        grid_cap[v] = std::max(1, s->stages ? yee_bulk_resident_ctas(s->rows, s->stages) : yee_resident_ctas(s->rows, v));
+        grid_cap[v] = std::max(1, s->stages ? yee_bulk_resident_ctas(s->rows, s->stages, true)
+                                            : yee_resident_ctas(s->rows, v));
     s->resident = grid_cap[4];
     auto clock = [&] { return (now_s() - t0); };
     auto arrived = [&](Inst *in, double t) { return time_scale <= 0 || in->t_arrival * time_scale <= t; };

@@ -83,6 +83,10 @@ struct ptk_solver {
     int *d_err = nullptr;      // raised by the staged kernel if a bounded wait expires
     void *d_tma = nullptr;     // tensor maps of the staged kernel (encoded for tma_by rows)
     int tma_by = 0;
+    unsigned char *mat = nullptr;   // material index of the coefficients (one byte per node)
+    float *mat_tab = nullptr;       // its table, kMaxMaterials x (Ca, Cb, Da, Db)
+    int nmat = 0;                   // materials in the table; 0 = per-cell arrays only
+    bool mat_enabled = true;
     int total_tiles = 0;
     InstDesc *d_desc = nullptr;
     int *d_tile0 = nullptr;
@@ -93,6 +97,27 @@ struct ptk_solver {
 };
 
 namespace ptk {
+
+// The staged kernel reads the material index when the coefficients have one and an instantiation
+// of the shape exists; otherwise the per-cell arrays, with the ring clamped to a dense shape.
+static bool use_mat(const ptk_solver *s)
+{
+    return s->stages > 0 && s->mat_enabled && s->nmat > 0 && yee_bulk_smem_bytes(s->by, s->stages, true) > 0;
+}
+
+static int run_stages(const ptk_solver *s)
+{
+    if (s->stages <= 0 || use_mat(s) || yee_bulk_smem_bytes(s->by, s->stages, false) > 0) return s->stages;
+    return 4;
+}
+
+static int rebuild_material(ptk_solver *s, cudaStream_t st)
+{
+    s->nmat = 0;
+    if (!s->mat_enabled) return PTK_OK;
+    const float *const c[4] = {s->coef[0], s->coef[1], s->coef[2], s->coef[3]};
+    return build_material_index(c, s->L, s->mat, s->mat_tab, &s->nmat, st);
+}
 
 static InstDesc host_desc(const ptk_solver *s, int steps_left)
 {
@@ -108,6 +133,11 @@ static InstDesc host_desc(const ptk_solver *s, int steps_left)
     d.nwave = s->nwave;
     d.step = s->step;
     d.steps_left = steps_left;
+    if (use_mat(s)) {
+        d.mat = s->mat;
+        d.mat_tab = s->mat_tab;
+        d.nmat = s->nmat;
+    }
     plan_tiles(d, s->by, s->kc, s->vec);
     return d;
 }
@@ -120,7 +150,9 @@ static int solver_sync_desc(ptk_solver *s, int steps_left, cudaStream_t st)
         if (s->tma_by != s->by) {
             // The arrays never move, so the maps change only with the tile rows.
             alignas(64) unsigned char maps[kTmaSetBytes];
-            int rc = encode_tma_set(d, s->by, maps);
+            InstDesc e = d;
+            e.mat = s->mat;   // the index map is always encoded; the kernel variant decides its use
+            int rc = encode_tma_set(e, s->by, maps);
             if (rc) return rc;
             PTK_CUDA_TRY(cudaStreamSynchronize(st));
             PTK_CUDA_TRY(cudaMemcpy(s->d_tma, maps, kTmaSetBytes, cudaMemcpyHostToDevice));
@@ -145,7 +177,9 @@ static void drop_graphs(ptk_solver *s)
 // Graph of `len` fused steps + one advance for this solver's current tile shape.
 static int solver_graph(ptk_solver *s, int len, cudaGraphExec_t *out)
 {
-    GraphKey key{len, s->by, s->kc, s->vec, s->stages};
+    const bool mat = use_mat(s);
+    const int stages = run_stages(s);
+    GraphKey key{len, s->by, s->kc, s->vec, stages * 2 + (mat ? 1 : 0)};
     auto it = s->graphs.find(key);
     if (it != s->graphs.end()) {
         *out = it->second;
@@ -156,9 +190,9 @@ static int solver_graph(ptk_solver *s, int len, cudaGraphExec_t *out)
     set_capturing(true);
     int rc = PTK_OK;
     for (int q = 0; q < len && rc == PTK_OK; ++q)
-        rc = s->stages > 0
-                 ? launch_yee_step_bulk(s->d_desc, s->d_tile0, 1, s->total_tiles, q, s->by, s->stages, 0, s->d_err,
-                                        s->cap)
+        rc = stages > 0
+                 ? launch_yee_step_bulk(s->d_desc, s->d_tile0, 1, s->total_tiles, q, s->by, stages, 0, s->d_err,
+                                        s->cap, nullptr, mat)
                  : launch_yee_step_v(s->d_desc, s->d_tile0, 1, s->total_tiles, q, s->by, s->vec, 0, s->cap);
     if (rc == PTK_OK) rc = launch_advance(s->d_desc, 1, len, s->cap);
     set_capturing(false);
@@ -245,6 +279,9 @@ int ptk_solver_create(const ptk_fdtd_params *p, ptk_solver **out)
     if (rc == PTK_OK) rc = pool_alloc(2 * sizeof(int), st, (void **)&s->d_tile0);
     if (rc == PTK_OK) rc = pool_alloc(sizeof(int), st, (void **)&s->d_err);
     if (rc == PTK_OK) rc = pool_alloc(kTmaSetBytes, st, &s->d_tma);
+    if (rc == PTK_OK) rc = pool_alloc((size_t)s->L.total, st, (void **)&s->mat);
+    if (rc == PTK_OK) rc = pool_alloc(sizeof(float) * 4 * kMaxMaterials, st, (void **)&s->mat_tab);
+    if (rc == PTK_OK) cudaMemsetAsync(s->mat, 0, (size_t)s->L.total, st);
     if (rc == PTK_OK && ((uintptr_t)s->d_tma & 63))
         rc = set_error(PTK_ERR_CUDA, "tensor-map buffer is not 64-byte aligned");
     if (rc == PTK_OK) cudaMemsetAsync(s->d_err, 0, sizeof(int), st);
@@ -283,6 +320,8 @@ int ptk_solver_destroy(ptk_solver *s)
         pool_free(s->d_tile0, st);
         pool_free(s->d_err, st);
         pool_free(s->d_tma, st);
+        pool_free(s->mat, st);
+        pool_free(s->mat_tab, st);
         if (s->cap) cudaStreamDestroy(s->cap);
     }
     cudaStreamSynchronize(st);
@@ -372,7 +411,7 @@ int ptk_solver_set_coefficients(ptk_solver *s, const float *Ca, const float *Cb,
         if (stage) pool_free(stage, st);
         if (rc) return rc;
     }
-    return PTK_OK;
+    return rebuild_material(s, st);
 }
 
 int ptk_solver_set_vacuum(ptk_solver *s, void *stream)
@@ -387,7 +426,7 @@ int ptk_solver_set_vacuum(ptk_solver *s, void *stream)
         int rc = launch_fill(s->coef[c], s->L.total, v[c], st);
         if (rc) return rc;
     }
-    return PTK_OK;
+    return rebuild_material(s, st);
 }
 
 int ptk_solver_set_source(ptk_solver *s, int i, int j, int k, const float *wave, int nwave, int where,
@@ -446,7 +485,7 @@ int ptk_solver_set_tiles(ptk_solver *s, const ptk_tile_config *cfg)
     if (vec == 0) vec = default_vec(s->p.Nx);
     PTK_CHECK_ARG(by == 4 || by == 8 || by == 16, "tile rows must be 4, 8 or 16 (got %d)", by);
     PTK_CHECK_ARG(vec == 1 || vec == 2 || vec == 4, "cells per thread must be 1, 2 or 4 (got %d)", vec);
-    PTK_CHECK_ARG(stages == 0 || yee_bulk_smem_bytes(by, stages) > 0,
+    PTK_CHECK_ARG(stages == 0 || yee_bulk_smem_bytes(by, stages, false) > 0 || yee_bulk_smem_bytes(by, stages, true) > 0,
                   "no staged kernel for %d rows with %d stages", by, stages);
     PTK_CHECK_ARG(kc >= 0, "tile depth must be >= 0");
     if (kc >= s->p.Nz) kc = 0;
@@ -454,6 +493,30 @@ int ptk_solver_set_tiles(ptk_solver *s, const ptk_tile_config *cfg)
     s->kc = kc;
     s->vec = vec;
     s->stages = stages;
+    return PTK_OK;
+}
+
+int ptk_solver_use_material_index(ptk_solver *s, int enable, void *stream)
+{
+    clear_error();
+    PTK_CHECK_ARG(s, "NULL solver");
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->mat_enabled = enable != 0;
+    return rebuild_material(s, S(stream));
+}
+
+int ptk_solver_material_count(const ptk_solver *s, int *nmat)
+{
+    PTK_CHECK_ARG(s && nmat, "NULL argument");
+    *nmat = s->mat_enabled ? s->nmat : 0;
+    return PTK_OK;
+}
+
+int ptk_solver_kernel(const ptk_solver *s, int *stages, int *material_index)
+{
+    PTK_CHECK_ARG(s && stages && material_index, "NULL argument");
+    *stages = run_stages(s);
+    *material_index = use_mat(s) ? 1 : 0;
     return PTK_OK;
 }
 
@@ -606,8 +669,12 @@ int ptk_autotune_tiles(int Nx, int Ny, int Nz, ptk_tile_config *best, float *bes
             if (32 * vec > 2 * std::max(Nx, 32)) continue;   // tiles far wider than the grid
             add(by, vec, 0, yee_resident_ctas(by, vec));
         }
-    const int staged[7][2] = {{4, 2}, {4, 3}, {4, 4}, {4, 5}, {8, 2}, {8, 3}, {8, 4}};
-    for (const auto &bs : staged) add(bs[0], 4, bs[1], yee_bulk_resident_ctas(bs[0], bs[1]));
+    // Staged shapes: timed on vacuum coefficients, i.e. with the material index where the shape has it.
+    const int staged[10][2] = {{4, 2}, {4, 3}, {4, 4}, {4, 5}, {4, 6}, {8, 2}, {8, 3}, {8, 4}, {8, 5}, {8, 6}};
+    for (const auto &bs : staged) {
+        const bool m = yee_bulk_smem_bytes(bs[0], bs[1], true) > 0;
+        add(bs[0], 4, bs[1], yee_bulk_resident_ctas(bs[0], bs[1], m));
+    }
     for (const ptk_tile_config &c : cands) {
         {
             if (ptk_solver_set_tiles(s, &c)) continue;

@@ -12,9 +12,15 @@
 // double-buffered shared array, and a stage is refilled only after the barrier that follows its
 // last reader.
 //
-// Tensor maps (one per array and parity: 6 fields x 2 + 4 coefficients) are encoded on the host
-// (cuTensorMapEncodeTiled through the runtime's driver entry point) into device memory; the issuing
-// lane acquire-fences a map before its first use in a tile.
+// With a material index (MAT instantiations) the four coefficient boxes of a plane become one box
+// of one-byte material ids (160 bytes wide, rows of the tile and its y-1 halo row), and each
+// thread looks its cells' (Ca, Cb, Da, Db) up in the instance's table of at most 256 entries,
+// copied into shared memory when a CTA starts a tile of another instance: 49 bytes of HBM traffic
+// per cell update instead of 64, same values, same results.
+//
+// Tensor maps (one per array and parity: 6 fields x 2, 4 coefficients, the material index) are
+// encoded on the host (cuTensorMapEncodeTiled through the runtime's driver entry point) into
+// device memory; the issuing lane acquire-fences a map before its first use in a tile.
 //
 // Waits on an mbarrier are bounded; on expiry the kernel raises *err (results of that launch are
 // then invalid and the host reports PTK_ERR_TIMEOUT).
@@ -29,42 +35,59 @@ namespace ptk {
 
 namespace {
 
-constexpr int kRowW = 136;      // staged row: x0-4 .. x0+131 (16-byte aligned ends)
+constexpr int kRowW = 136;      // staged float row: x0-4 .. x0+131 (16-byte aligned ends)
+constexpr int kRowB8 = 160;     // staged material-index row (bytes): x0-16 .. x0+143
 constexpr int kWaitLimit = 1 << 22;
+constexpr int kMapMat = 16;     // tensor map of the material index in an instance's set
+constexpr size_t kTabBytes = 256 * sizeof(float4);   // material table (Ca, Cb, Da, Db) per entry
 
-// Arrays in stage order and the frame rows r (j = y0 - 1 + r) each one needs.
-enum { A_HX, A_HY, A_HZ, A_EX, A_EY, A_EZ, A_CA, A_CB, A_DA, A_DB, A_N };
+// Arrays in stage order and the frame rows r (j = y0 - 1 + r) each one needs.  With per-cell
+// coefficient arrays the stage holds Ca, Cb, Da, Db; with a material index (MAT) one byte per
+// node (rows 0..BY) replaces all four and the values come from a table in shared memory.
+enum { A_HX, A_HY, A_HZ, A_EX, A_EY, A_EZ, A_CA, A_CB, A_DA, A_DB };
+constexpr int A_MT = 6;
 
-__host__ __device__ constexpr int row_lo(int a) { return (a == A_HY || a == A_CA || a == A_CB) ? 1 : 0; }
+template <bool MAT>
+__host__ __device__ constexpr int n_arrays() { return MAT ? 7 : 10; }
+template <bool MAT>
+__host__ __device__ constexpr bool is_u8(int a) { return MAT && a == A_MT; }
+template <bool MAT>
+__host__ __device__ constexpr int row_lo(int a) { return (a == A_HY || (!MAT && (a == A_CA || a == A_CB))) ? 1 : 0; }
 template <int BY>
 __host__ __device__ constexpr int row_hi(int a) { return (a == A_EX || a == A_EZ) ? BY + 2 : BY + 1; }
-template <int BY>
-__host__ __device__ constexpr int rows_of(int a) { return row_hi<BY>(a) - row_lo(a); }
+template <int BY, bool MAT>
+__host__ __device__ constexpr int rows_of(int a) { return row_hi<BY>(a) - row_lo<MAT>(a); }
+template <bool MAT>
+__host__ __device__ constexpr int row_bytes(int a) { return is_u8<MAT>(a) ? kRowB8 : kRowW * 4; }
 // Each array's region in a stage starts on a 128-byte boundary (TMA destination alignment).
-template <int BY>
-__host__ __device__ constexpr int region_bytes(int a) { return (rows_of<BY>(a) * kRowW * 4 + 127) / 128 * 128; }
-template <int BY>
+template <int BY, bool MAT>
+__host__ __device__ constexpr int region_bytes(int a) { return (rows_of<BY, MAT>(a) * row_bytes<MAT>(a) + 127) / 128 * 128; }
+template <int BY, bool MAT>
 __host__ __device__ constexpr int region_off(int a)
 {
     int o = 0;
-    for (int q = 0; q < a; ++q) o += region_bytes<BY>(q);
+    for (int q = 0; q < a; ++q) o += region_bytes<BY, MAT>(q);
     return o;
 }
-template <int BY>
-__host__ __device__ constexpr size_t stage_bytes() { return (size_t)region_off<BY>(A_N); }
-template <int BY>
-__host__ __device__ constexpr uint32_t box_bytes(int a) { return (uint32_t)(rows_of<BY>(a) * kRowW * 4); }
-template <int BY>
+template <int BY, bool MAT>
+__host__ __device__ constexpr size_t stage_bytes() { return (size_t)region_off<BY, MAT>(n_arrays<MAT>()); }
+template <int BY, bool MAT>
+__host__ __device__ constexpr uint32_t box_bytes(int a) { return (uint32_t)(rows_of<BY, MAT>(a) * row_bytes<MAT>(a)); }
+template <int BY, bool MAT>
 __host__ __device__ constexpr uint32_t plane_tx_bytes()
 {
     uint32_t t = 0;
-    for (int a = 0; a < A_N; ++a) t += box_bytes<BY>(a);
+    for (int a = 0; a < n_arrays<MAT>(); ++a) t += box_bytes<BY, MAT>(a);
     return t;
 }
 template <int BY>
 __host__ __device__ constexpr size_t xchg_bytes() { return (size_t)2 * 2 * (BY + 1) * 32 * sizeof(float4); }
-template <int BY, int S>
-__host__ __device__ constexpr size_t smem_bytes() { return S * stage_bytes<BY>() + xchg_bytes<BY>() + S * 8 + 16; }
+// [S stages][H exchange][material table (MAT)][S mbarriers][tile slot]
+template <int BY, int S, bool MAT>
+__host__ __device__ constexpr size_t smem_bytes()
+{
+    return S * stage_bytes<BY, MAT>() + xchg_bytes<BY>() + (MAT ? kTabBytes : 0) + S * 8 + 16;
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -120,43 +143,55 @@ __device__ __forceinline__ float yee_b(float d, float h, float c, float a1, floa
     return __fadd_rn(__fmul_rn(d, h), __fmul_rn(c, curl));
 }
 
-// Map of array a for field parity par in an instance's 16-map set.
+// Map of array a for field parity par in an instance's map set.
+template <bool MAT>
 __device__ __forceinline__ const CUtensorMap *map_of(const CUtensorMap *set, int a, int par)
 {
-    return a < 6 ? set + par * 6 + a : set + 12 + (a - 6);
+    return a < 6 ? set + par * 6 + a : (MAT ? set + kMapMat : set + 12 + (a - 6));
 }
 
-// Issue plane k of the tile into stage buffer `st` (called by the 32 lanes of one warp; lanes
-// 0..9 each issue one array's box).
-template <int BY>
+// Issue plane k of the tile into stage buffer `st` (called by the 32 lanes of one warp; lane a
+// issues array a's box).
+template <int BY, bool MAT>
 __device__ __forceinline__ void issue_plane(const CUtensorMap *set, int par, int x0, int y0, int k, bool next_only,
                                             unsigned char *st, uint64_t *bar, int lane)
 {
     if (lane == 0)
-        mbar_expect_tx(bar, next_only ? box_bytes<BY>(A_EX) + box_bytes<BY>(A_EY) : plane_tx_bytes<BY>());
+        mbar_expect_tx(bar, next_only ? box_bytes<BY, MAT>(A_EX) + box_bytes<BY, MAT>(A_EY) : plane_tx_bytes<BY, MAT>());
     __syncwarp();
-    if (lane < A_N && (!next_only || lane == A_EX || lane == A_EY))
-        tma_load_3d(st + region_off<BY>(lane), map_of(set, lane, par), x0 - 4, y0 - 1 + row_lo(lane), k, bar);
+    if (lane < n_arrays<MAT>() && (!next_only || lane == A_EX || lane == A_EY))
+        tma_load_3d(st + region_off<BY, MAT>(lane), map_of<MAT>(set, lane, par), is_u8<MAT>(lane) ? x0 - 16 : x0 - 4,
+                    y0 - 1 + row_lo<MAT>(lane), k, bar);
 }
 
-template <int BY>
+template <int BY, bool MAT>
 __device__ __forceinline__ const float *row_ptr(const unsigned char *st, int a, int r)
 {
-    return reinterpret_cast<const float *>(st + region_off<BY>(a)) + (size_t)(r - row_lo(a)) * kRowW;
+    return reinterpret_cast<const float *>(st + region_off<BY, MAT>(a)) + (size_t)(r - row_lo<MAT>(a)) * kRowW;
+}
+
+// Material-index row of frame row r; byte 16 + c is the node at x0 + c.
+template <int BY>
+__device__ __forceinline__ const unsigned char *row_mat(const unsigned char *st, int r)
+{
+    return st + region_off<BY, true>(A_MT) + (size_t)r * kRowB8;
 }
 
 }  // namespace
 
-template <int BY, int S>
+template <int BY, int S, bool MAT>
 __global__ void __launch_bounds__(32 * (BY + 1), 1)
 k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile0, int ninst, int s_off,
                 int total_tiles, int *err, int *work)
 {
+    constexpr size_t SB = stage_bytes<BY, MAT>();
     extern __shared__ __align__(128) unsigned char smem[];
     unsigned char *stages = smem;
-    float4 *xchg = reinterpret_cast<float4 *>(smem + S * stage_bytes<BY>());   // [2 buf][2 arr][BY+1][32]
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + S * stage_bytes<BY>() + xchg_bytes<BY>());
+    float4 *xchg = reinterpret_cast<float4 *>(smem + S * SB);   // [2 buf][2 arr][BY+1][32]
+    float4 *tab = reinterpret_cast<float4 *>(smem + S * SB + xchg_bytes<BY>());   // MAT: (Ca, Cb, Da, Db)[256]
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + S * SB + xchg_bytes<BY>() + (MAT ? kTabBytes : 0));
     int *slot = reinterpret_cast<int *>(bars + S);   // next tile, handed to the whole CTA
+    const void *tab_src = nullptr;                   // instance whose table is loaded (MAT)
 
     const int lane = threadIdx.x, ty = threadIdx.y;
     if (smem_u32(smem) & 127u) {   // TMA destinations need 128-byte alignment: refuse, do not fault
@@ -203,6 +238,15 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
         const long long plane = D->plane;
         const float cx = D->cx, cy = D->cy, cz = D->cz;
         const CUtensorMap *maps = reinterpret_cast<const CUtensorMap *>(D->tma);
+        if constexpr (MAT) {
+            // The previous tile ended with a block barrier: nobody reads the old table any more.
+            if (D->mat_tab != tab_src) {
+                const float4 *src_tab = reinterpret_cast<const float4 *>(D->mat_tab);
+                for (int m = ty * 32 + lane; m < D->nmat; m += 32 * (BY + 1)) tab[m] = __ldg(src_tab + m);
+                tab_src = D->mat_tab;
+                __syncthreads();
+            }
+        }
         float *__restrict__ oHx = D->buf[par ^ 1][0];
         float *__restrict__ oHy = D->buf[par ^ 1][1];
         float *__restrict__ oHz = D->buf[par ^ 1][2];
@@ -223,11 +267,11 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
 
         // prologue: the first S planes
         if (ty == 0) {
-            if (lane < A_N) tma_acquire(map_of(maps, lane, par));
+            if (lane < n_arrays<MAT>()) tma_acquire(map_of<MAT>(maps, lane, par));
             for (int q = 0; q < S && q < nplanes; ++q) {
                 const unsigned G = gbase + q;
-                issue_plane<BY>(maps, par, x0, y0, kstart + q, kstart + q == k1, stages + (size_t)(G % S) * stage_bytes<BY>(),
-                                &bars[G % S], lane);
+                issue_plane<BY, MAT>(maps, par, x0, y0, kstart + q, kstart + q == k1, stages + (size_t)(G % S) * SB,
+                                     &bars[G % S], lane);
             }
         }
 
@@ -247,8 +291,8 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
         for (int k = kstart; k < k1; ++k, off += plane) {
             const int q = k - kstart;
             const unsigned Gc = gbase + q, Gn = Gc + 1;
-            const unsigned char *cur = stages + (size_t)(Gc % S) * stage_bytes<BY>();
-            const unsigned char *nxt = stages + (size_t)(Gn % S) * stage_bytes<BY>();
+            const unsigned char *cur = stages + (size_t)(Gc % S) * SB;
+            const unsigned char *nxt = stages + (size_t)(Gn % S) * SB;
             if (!failed) {
                 bool ok = mbar_wait(&bars[Gc % S], (Gc / S) & 1);
                 ok = ok && mbar_wait(&bars[Gn % S], (Gn / S) & 1);
@@ -263,25 +307,38 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
             float ez_l = 0.f, ey_l = 0.f;
             const bool act = xin && (halo ? (jrow && !warm) : jrow);
             if (act) {
-                hx = ld4s(row_ptr<BY>(cur, A_HX, r) + xl);
-                ez = ld4s(row_ptr<BY>(cur, A_EZ, r) + xl);
-                ex0 = ld4s(row_ptr<BY>(cur, A_EX, r) + xl);
-                ey0 = ld4s(row_ptr<BY>(cur, A_EY, r) + xl);
-                ey1 = ld4s(row_ptr<BY>(nxt, A_EY, r) + xl);
-                exj1 = ld4s(row_ptr<BY>(cur, A_EX, r + 1) + xl);
-                ezj1 = ld4s(row_ptr<BY>(cur, A_EZ, r + 1) + xl);
-                da = ld4s(row_ptr<BY>(cur, A_DA, r) + xl);
-                db = ld4s(row_ptr<BY>(cur, A_DB, r) + xl);
-                hz = ld4s(row_ptr<BY>(cur, A_HZ, r) + xl);
+                hx = ld4s(row_ptr<BY, MAT>(cur, A_HX, r) + xl);
+                ez = ld4s(row_ptr<BY, MAT>(cur, A_EZ, r) + xl);
+                ex0 = ld4s(row_ptr<BY, MAT>(cur, A_EX, r) + xl);
+                ey0 = ld4s(row_ptr<BY, MAT>(cur, A_EY, r) + xl);
+                ey1 = ld4s(row_ptr<BY, MAT>(nxt, A_EY, r) + xl);
+                exj1 = ld4s(row_ptr<BY, MAT>(cur, A_EX, r + 1) + xl);
+                ezj1 = ld4s(row_ptr<BY, MAT>(cur, A_EZ, r + 1) + xl);
+                hz = ld4s(row_ptr<BY, MAT>(cur, A_HZ, r) + xl);
+                if constexpr (MAT) {
+                    // four material ids, one per cell, then their (Ca, Cb, Da, Db) from the table
+                    const uint32_t ids = *reinterpret_cast<const uint32_t *>(row_mat<BY>(cur, r) + 16 + 4 * lane);
+                    const float4 m0 = tab[ids & 255u], m1 = tab[(ids >> 8) & 255u];
+                    const float4 m2 = tab[(ids >> 16) & 255u], m3 = tab[ids >> 24];
+                    ca = make_float4(m0.x, m1.x, m2.x, m3.x);
+                    cb = make_float4(m0.y, m1.y, m2.y, m3.y);
+                    da = make_float4(m0.z, m1.z, m2.z, m3.z);
+                    db = make_float4(m0.w, m1.w, m2.w, m3.w);
+                } else {
+                    da = ld4s(row_ptr<BY, MAT>(cur, A_DA, r) + xl);
+                    db = ld4s(row_ptr<BY, MAT>(cur, A_DB, r) + xl);
+                }
                 if (!halo) {
-                    hy = ld4s(row_ptr<BY>(cur, A_HY, r) + xl);
-                    ex1 = ld4s(row_ptr<BY>(nxt, A_EX, r) + xl);
-                    ca = ld4s(row_ptr<BY>(cur, A_CA, r) + xl);
-                    cb = ld4s(row_ptr<BY>(cur, A_CB, r) + xl);
+                    hy = ld4s(row_ptr<BY, MAT>(cur, A_HY, r) + xl);
+                    ex1 = ld4s(row_ptr<BY, MAT>(nxt, A_EX, r) + xl);
+                    if constexpr (!MAT) {
+                        ca = ld4s(row_ptr<BY, MAT>(cur, A_CA, r) + xl);
+                        cb = ld4s(row_ptr<BY, MAT>(cur, A_CB, r) + xl);
+                    }
                 }
                 if (lane == 31) {
-                    ez_l = row_ptr<BY>(cur, A_EZ, r)[xl + 4];
-                    ey_l = row_ptr<BY>(cur, A_EY, r)[xl + 4];
+                    ez_l = row_ptr<BY, MAT>(cur, A_EZ, r)[xl + 4];
+                    ey_l = row_ptr<BY, MAT>(cur, A_EY, r)[xl + 4];
                 }
             }
             // x+1 neighbours
@@ -305,13 +362,21 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
             }
             float hyh = 0.f, hzh = 0.f;   // halo column x0-1
             if (hcol && !warm) {
-                const float *Hy = row_ptr<BY>(cur, A_HY, r), *Hz = row_ptr<BY>(cur, A_HZ, r);
-                const float *Ez = row_ptr<BY>(cur, A_EZ, r), *Ex = row_ptr<BY>(cur, A_EX, r);
-                const float *Exn = row_ptr<BY>(nxt, A_EX, r), *Exj = row_ptr<BY>(cur, A_EX, r + 1);
-                const float *Ey = row_ptr<BY>(cur, A_EY, r), *Da = row_ptr<BY>(cur, A_DA, r);
-                const float *Db = row_ptr<BY>(cur, A_DB, r);
-                hyh = yee_b(Da[3], Hy[3], Db[3], ez.x, Ez[3], cx, Exn[3], Ex[3], cz);
-                hzh = yee_b(Da[3], Hz[3], Db[3], Exj[3], Ex[3], cy, ey0.x, Ey[3], cx);
+                const float *Hy = row_ptr<BY, MAT>(cur, A_HY, r), *Hz = row_ptr<BY, MAT>(cur, A_HZ, r);
+                const float *Ez = row_ptr<BY, MAT>(cur, A_EZ, r), *Ex = row_ptr<BY, MAT>(cur, A_EX, r);
+                const float *Exn = row_ptr<BY, MAT>(nxt, A_EX, r), *Exj = row_ptr<BY, MAT>(cur, A_EX, r + 1);
+                const float *Ey = row_ptr<BY, MAT>(cur, A_EY, r);
+                float dah, dbh;   // coefficients of node x0-1
+                if constexpr (MAT) {
+                    const float4 mh = tab[row_mat<BY>(cur, r)[15]];
+                    dah = mh.z;
+                    dbh = mh.w;
+                } else {
+                    dah = row_ptr<BY, MAT>(cur, A_DA, r)[3];
+                    dbh = row_ptr<BY, MAT>(cur, A_DB, r)[3];
+                }
+                hyh = yee_b(dah, Hy[3], dbh, ez.x, Ez[3], cx, Exn[3], Ex[3], cz);
+                hzh = yee_b(dah, Hz[3], dbh, Exj[3], Ex[3], cy, ey0.x, Ey[3], cx);
             }
             float4 *sH = xchg + (size_t)(q & 1) * 2 * (BY + 1) * 32;   // [arr][row][lane]
             if (!warm) {
@@ -323,8 +388,8 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
             // before this one, and nothing after this barrier reads a stage: refill it now.
             if (ty == 0 && q + S < nplanes) {
                 const unsigned G = gbase + q + S;
-                issue_plane<BY>(maps, par, x0, y0, kstart + q + S, kstart + q + S == k1,
-                                stages + (size_t)(G % S) * stage_bytes<BY>(), &bars[G % S], lane);
+                issue_plane<BY, MAT>(maps, par, x0, y0, kstart + q + S, kstart + q + S == k1, stages + (size_t)(G % S) * SB,
+                                     &bars[G % S], lane);
             }
             float hy_p = __shfl_up_sync(0xffffffffu, hyn[3], 1);
             float hz_p = __shfl_up_sync(0xffffffffu, hzn[3], 1);
@@ -385,75 +450,79 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
 }
 
 // Opt the instantiation into its dynamic shared memory (once per process; repeating it is harmless).
-template <int BY, int S>
+template <int BY, int S, bool MAT>
 static int prepare_bulk()
 {
     static bool attr_set = false;
     if (!attr_set) {
-        PTK_CUDA_TRY(cudaFuncSetAttribute(k_yee_step_bulk<BY, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)smem_bytes<BY, S>()));
+        PTK_CUDA_TRY(cudaFuncSetAttribute(k_yee_step_bulk<BY, S, MAT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem_bytes<BY, S, MAT>()));
         attr_set = true;
     }
     return PTK_OK;
 }
 
-template <int BY, int S>
+template <int BY, int S, bool MAT>
 static int resident_bulk()
 {
-    if (prepare_bulk<BY, S>()) return 0;
+    if (prepare_bulk<BY, S, MAT>()) return 0;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_yee_step_bulk<BY, S>, 32 * (BY + 1),
-                                                      smem_bytes<BY, S>()) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_yee_step_bulk<BY, S, MAT>, 32 * (BY + 1),
+                                                      smem_bytes<BY, S, MAT>()) != cudaSuccess)
         return 0;
     return per_sm * std::max(1, sm_count());
 }
 
-template <int BY, int S>
+template <int BY, int S, bool MAT>
 static int launch_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles, int s_offset,
                        int grid, int *err, int *work, cudaStream_t s)
 {
-    const size_t smem = smem_bytes<BY, S>();
-    int rc = prepare_bulk<BY, S>();
+    const size_t smem = smem_bytes<BY, S, MAT>();
+    int rc = prepare_bulk<BY, S, MAT>();
     if (rc) return rc;
     const int g = (grid <= 0 || grid > total_tiles) ? total_tiles : grid;
-    k_yee_step_bulk<BY, S><<<g, dim3(32, BY + 1), smem, s>>>(d_insts, d_tile0, ninst, s_offset, total_tiles, err,
-                                                             work);
+    k_yee_step_bulk<BY, S, MAT><<<g, dim3(32, BY + 1), smem, s>>>(d_insts, d_tile0, ninst, s_offset, total_tiles,
+                                                                  err, work);
     PTK_CUDA_TRY(cudaGetLastError());
     count_launches(1);
     return PTK_OK;
 }
 
-// Rings of at least 2 stages: plane q waits for the stage of plane q+1 before its barrier, and the
-// stage of plane q+1 is issued after the barrier of plane q+1-S, so q+1-S <= q-1.
+// Instantiated shapes (rows, ring stages).  Rings of at least 2 stages: plane q waits for the stage
+// of plane q+1 before its barrier, and the stage of plane q+1 is issued after the barrier of plane
+// q+1-S, so q+1-S <= q-1.  The material-index stages are smaller, so deeper rings fit.
+#define PTK_DENSE_SHAPES(X) X(4, 2, false) X(4, 3, false) X(4, 4, false) X(4, 5, false) \
+    X(8, 2, false) X(8, 3, false) X(8, 4, false)
+#define PTK_MAT_SHAPES(X) X(4, 2, true) X(4, 3, true) X(4, 4, true) X(4, 5, true) X(4, 6, true) \
+    X(8, 2, true) X(8, 3, true) X(8, 4, true) X(8, 5, true) X(8, 6, true)
+
 int launch_yee_step_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles, int s_offset,
-                         int by, int stages, int grid, int *err, cudaStream_t s, int *work)
+                         int by, int stages, int grid, int *err, cudaStream_t s, int *work, bool mat)
 {
     if (total_tiles <= 0) return PTK_OK;
-#define PTK_BULK(B, S)                                                                                  \
-    if (by == B && stages == S)                                                                         \
-        return launch_bulk<B, S>(d_insts, d_tile0, ninst, total_tiles, s_offset, grid, err, work, s);
-    PTK_BULK(4, 2) PTK_BULK(4, 3) PTK_BULK(4, 4) PTK_BULK(4, 5)
-    PTK_BULK(8, 2) PTK_BULK(8, 3) PTK_BULK(8, 4)
+#define PTK_BULK(B, S, M)                                                                               \
+    if (by == B && stages == S && mat == M)                                                             \
+        return launch_bulk<B, S, M>(d_insts, d_tile0, ninst, total_tiles, s_offset, grid, err, work, s);
+    PTK_DENSE_SHAPES(PTK_BULK) PTK_MAT_SHAPES(PTK_BULK)
 #undef PTK_BULK
-    return set_error(PTK_ERR_INVALID, "no staged kernel for %d rows x %d stages", by, stages);
+    return set_error(PTK_ERR_INVALID, "no staged kernel for %d rows x %d stages%s", by, stages,
+                     mat ? " with a material index" : "");
 }
 
-size_t yee_bulk_smem_bytes(int by, int stages)
+size_t yee_bulk_smem_bytes(int by, int stages, bool mat)
 {
-#define PTK_SM(B, S) \
-    if (by == B && stages == S) return smem_bytes<B, S>();
-    PTK_SM(4, 2) PTK_SM(4, 3) PTK_SM(4, 4) PTK_SM(4, 5)
-    PTK_SM(8, 2) PTK_SM(8, 3) PTK_SM(8, 4)
+#define PTK_SM(B, S, M) \
+    if (by == B && stages == S && mat == M) return smem_bytes<B, S, M>();
+    PTK_DENSE_SHAPES(PTK_SM) PTK_MAT_SHAPES(PTK_SM)
 #undef PTK_SM
     return 0;
 }
 
-int yee_bulk_resident_ctas(int by, int stages)
+int yee_bulk_resident_ctas(int by, int stages, bool mat)
 {
-#define PTK_RES(B, S) \
-    if (by == B && stages == S) return resident_bulk<B, S>();
-    PTK_RES(4, 2) PTK_RES(4, 3) PTK_RES(4, 4) PTK_RES(4, 5)
-    PTK_RES(8, 2) PTK_RES(8, 3) PTK_RES(8, 4)
+#define PTK_RES(B, S, M) \
+    if (by == B && stages == S && mat == M) return resident_bulk<B, S, M>();
+    PTK_DENSE_SHAPES(PTK_RES) PTK_MAT_SHAPES(PTK_RES)
 #undef PTK_RES
     return 0;
 }
@@ -483,14 +552,18 @@ static int encode_set(const InstDesc &d, CUtensorMap *out)
     if (!enc) return set_error(PTK_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
     const cuuint64_t dims[3] = {(cuuint64_t)d.pitch, (cuuint64_t)d.ny + 1, (cuuint64_t)d.nz + 1};
     const cuuint64_t strides[2] = {(cuuint64_t)d.pitch * 4, (cuuint64_t)d.plane * 4};
+    const cuuint64_t strides8[2] = {(cuuint64_t)d.pitch, (cuuint64_t)d.plane};
     const cuuint32_t estr[3] = {1, 1, 1};
-    for (int m = 0; m < 16; ++m) {
-        const int a = m < 12 ? m % 6 : 6 + (m - 12);
-        void *base = m < 12 ? (void *)d.buf[m / 6][m % 6] : (void *)d.coef[m - 12];
-        const cuuint32_t box[3] = {(cuuint32_t)kRowW, (cuuint32_t)rows_of<BY>(a), 1};
-        CUresult r = enc(&out[m], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, estr,
-                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    // maps 0..11: the fields of both parities; 12..15: Ca, Cb, Da, Db; 16: the material index
+    for (int m = 0; m < 17; ++m) {
+        if (m == kMapMat && !d.mat) break;
+        const bool u8 = m == kMapMat;
+        const int a = m < 12 ? m % 6 : (u8 ? A_MT : 6 + (m - 12));
+        void *base = m < 12 ? (void *)d.buf[m / 6][m % 6] : u8 ? (void *)d.mat : (void *)d.coef[m - 12];
+        const cuuint32_t box[3] = {(cuuint32_t)(u8 ? kRowB8 : kRowW), (cuuint32_t)(u8 ? rows_of<BY, true>(a) : rows_of<BY, false>(a)), 1};
+        CUresult r = enc(&out[m], u8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims,
+                         u8 ? strides8 : strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (r != CUDA_SUCCESS) return set_error(PTK_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d) for map %d", (int)r, m);
     }
     return PTK_OK;

@@ -73,11 +73,24 @@ struct InstDesc {
     int tiles_x, tiles_y, tiles_z, face_tiles;
     int kc;                    // z-planes per main tile
     int vec;                   // x cells per thread: main tiles are 32*vec cells wide
-    const void *tma;           // staged kernel only: 16 tensor maps (6 fields x 2 parities, 4 coefs)
+    const void *tma;           // staged kernel only: tensor maps (6 fields x 2 parities, 4 coefs, index)
+    const unsigned char *mat;  // material index (padded layout, one byte per node), or null
+    const float *mat_tab;      // its table: nmat entries of (Ca, Cb, Da, Db)
+    int nmat;
 };
 
-// Bytes of one instance's tensor-map set (16 CUtensorMap of 128 bytes; 64-byte alignment).
-constexpr size_t kTmaSetBytes = 16 * 128;
+// Bytes of one instance's tensor-map set (17 CUtensorMap of 128 bytes; 64-byte alignment).
+constexpr size_t kTmaSetBytes = 17 * 128;
+// Material table entries (one-byte ids).
+constexpr int kMaxMaterials = 256;
+
+// Per-node material index of an instance's padded coefficient arrays (Ca, Cb, Da, Db): the
+// distinct tuples of the nodes (i <= Nx, j <= Ny, k <= Nz; row padding excluded) are gathered on
+// the device; if there are at most kMaxMaterials of them, `mat` (L.total bytes, padding left as
+// is) receives each node's id and `tab` (kMaxMaterials x 4 floats) the tuples, and *nmat their
+// count; otherwise *nmat = 0 and nothing else is written.  Synchronises `s`.
+int build_material_index(const float *const coef[4], const Layout &L, unsigned char *mat, float *tab, int *nmat,
+                         cudaStream_t s);
 // Encode the tensor maps of `d`'s arrays for the staged kernel with `by` tile rows into host
 // memory (kTmaSetBytes).
 int encode_tma_set(const InstDesc &d, int by, void *host_out);
@@ -104,12 +117,15 @@ int launch_yee_step_v(const InstDesc *d_insts, const int *d_tile0, int ninst, in
 // The staged variant (operands brought into shared memory by TMA tensor copies, `stages` planes
 // in a ring; 128-wide tiles, vec == 4; every instance's `tma` set encoded for `by`).  *err is
 // raised if a bounded wait expires.  With `work` (one zeroed counter per step offset), CTAs past
-// the first wave take tiles in list order as they free up instead of a static stride.
+// the first wave take tiles in list order as they free up instead of a static stride.  With `mat`
+// every instance carries a material index (and its map) and the coefficients come from its table.
 int launch_yee_step_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles, int s_offset,
-                         int by, int stages, int grid, int *err, cudaStream_t s, int *work = nullptr);
-size_t yee_bulk_smem_bytes(int by, int stages);
+                         int by, int stages, int grid, int *err, cudaStream_t s, int *work = nullptr,
+                         bool mat = false);
+// Shared memory of a staged instantiation (0: no such kernel).
+size_t yee_bulk_smem_bytes(int by, int stages, bool mat = false);
 // CTAs of the staged kernel that fit on the whole GPU at once (0: no such kernel).
-int yee_bulk_resident_ctas(int by, int stages);
+int yee_bulk_resident_ctas(int by, int stages, bool mat = false);
 // Z depths (at most `n`, best first) whose tile count fills whole waves of `resident` CTAs with the
 // least work per CTA: each CTA's cost is its planes plus the warm plane and the pipeline fill.
 int balanced_depths(int nx, int ny, int nz, int by, int vec, int resident, int *out, int n);

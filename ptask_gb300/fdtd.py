@@ -137,6 +137,12 @@ class Solver:
     def set_fields_device(self, ptrs, stream=None) -> None:
         call("ptk_solver_set_fields", self._h, _ptr_array(ptrs), PTK_DEVICE, stream)
 
+    def set_coefficients(self, Ca, Cb, Da, Db, stream=None) -> None:
+        """Per-cell coefficient arrays (Nx*Ny*Nz floats each, reference layout)."""
+        arrs = [np.ascontiguousarray(a, np.float32) for a in (Ca, Cb, Da, Db)]
+        call("ptk_solver_set_coefficients", self._h, *[a.ctypes.data for a in arrs], PTK_HOST, stream)
+        call("ptk_stream_sync", stream)
+
     def set_problem(self, prob: Problem, stream=None) -> None:
         arrs = [np.ascontiguousarray(a, np.float32) for a in (prob.Ca, prob.Cb, prob.Da, prob.Db)]
         call("ptk_solver_set_coefficients", self._h, *[a.ctypes.data for a in arrs], PTK_HOST, stream)
@@ -155,6 +161,21 @@ class Solver:
         (1, 2, 4; 0 = chosen from Nx), `stages` > 0 selects the kernel whose operands are staged in
         shared memory by TMA tensor copies (that many planes in the ring, 2..5)."""
         call("ptk_solver_set_tiles", self._h, C.byref(TileConfig(by, kc, vec, stages)))
+
+    def use_material_index(self, enable: bool = True, stream=None) -> None:
+        """Read the coefficients through a one-byte material index (default) or the per-cell arrays."""
+        call("ptk_solver_use_material_index", self._h, int(bool(enable)), stream)
+
+    def material_count(self) -> int:
+        n = C.c_int()
+        call("ptk_solver_material_count", self._h, C.byref(n))
+        return n.value
+
+    def kernel(self) -> tuple[int, bool]:
+        """(ring stages of the next run's step kernel, 0 = register kernel; reads the material index)"""
+        st, m = C.c_int(), C.c_int()
+        call("ptk_solver_kernel", self._h, C.byref(st), C.byref(m))
+        return st.value, bool(m.value)
 
     def tiles(self) -> tuple[int, int, int, int]:
         t = TileConfig()

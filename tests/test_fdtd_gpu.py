@@ -303,6 +303,58 @@ def test_staged_kernel_small_and_edge_shapes(shape):
             assert_parity(s.get_fields(), ref, f"staged {shape} by={by} stages={stages}")
 
 
+# ------------------------------------------------------------------------------------------------
+# Material index: one byte per node + a table instead of the four coefficient arrays.
+# ------------------------------------------------------------------------------------------------
+@pytest.mark.parametrize("by,stages", [(8, 4), (8, 6), (4, 3), (4, 5), (8, 2)])
+def test_material_index_equals_per_cell_arrays(by, stages):
+    shape, steps = (261, 37, 23), 7
+    pr = P.Problem.generate(*shape, n_boxes=5, eps=(1, 10), box=(5, 30), steps=steps, seed=15)
+    f = P.random_fields(*shape, seed=73, scale=1e-2)
+    ref = oracle.step_ext_f32(f, steps, pr.params, pr.Ca, pr.Cb, pr.Da, pr.Db, pr.src, pr.wave)
+    outs = []
+    for use in (True, False):
+        with P.Solver(pr.params) as s:
+            s.set_tiles(by, 5, 4, stages)
+            s.set_problem(pr)
+            s.use_material_index(use)
+            assert (s.material_count() > 0) == use and s.material_count() <= 6
+            st, mat = s.kernel()
+            assert mat == use and st == (stages if (use or stages <= 4) else 4)
+            s.set_fields(f)
+            s.run(steps)
+            outs.append(s.get_fields())
+    assert_parity(outs[0], ref, f"material index by={by} stages={stages}")
+    assert_parity(outs[1], ref, f"per-cell arrays by={by} stages={stages}")
+
+
+def coefficient_set(shape, k, seed):
+    """Coefficients with exactly k distinct (Ca, Cb, Da, Db) tuples, spread over the cells."""
+    p = P.reference_params(*shape)
+    n = shape[0] * shape[1] * shape[2]
+    rng = np.random.default_rng(seed)
+    ids = rng.permutation(np.arange(n) % k).reshape(shape[::-1])
+    cb = (np.float32(p.Dt / p.eps0) * (1 + np.arange(k, dtype=np.float32) / np.float32(512)))[ids]
+    one = np.ones(shape[::-1], np.float32)
+    return p, one, cb.astype(np.float32), one.copy(), one * np.float32(p.Dt / p.mu0)
+
+
+@pytest.mark.parametrize("k,expect", [(1, 1), (256, 256), (257, 0), (5000, 0)])
+def test_material_count_limit_and_fallback(k, expect):
+    shape, steps = (40, 30, 20), 5
+    p, ca, cb, da, db = coefficient_set(shape, k, seed=k)
+    f = P.random_fields(*shape, seed=74, scale=1e-2)
+    with P.Solver(p) as s:
+        s.set_tiles(8, 0, 4, 4)
+        s.set_coefficients(ca, cb, da, db)
+        assert s.material_count() == expect
+        assert s.kernel() == (4, expect > 0)
+        s.set_fields(f)
+        s.run(steps)
+        got = s.get_fields()
+    assert_parity(got, oracle.step_ext_f32(f, steps, p, ca, cb, da, db), f"{k} materials")
+
+
 def test_staged_full_size_matches_register_kernel(full_problem):
     pr = full_problem
     f = P.zero_fields(*FULL)
