@@ -37,6 +37,7 @@ sys.path.insert(0, str(ROOT))
 import numpy as np  # noqa: E402
 
 BYTES_PER_CELL = 64          # 6 fields read + written (48 B) + 4 coefficients read (16 B), FP32
+BYTES_PER_CELL_MAT = 49      # 6 fields read + written (48 B) + a one-byte material id (coefficients from a table)
 FALLBACK_HBM_GBS = 6800.0
 
 WORKLOADS = {
@@ -153,9 +154,10 @@ def hbm_peak():
     return FALLBACK_HBM_GBS, "fallback"
 
 
-def traffic_per_cell(kernel: str):
+def traffic_per_cell(kernel: str, mat: bool = False):
     """DRAM bytes per cell update of the given fused step kernel from its committed ncu summary."""
-    f = ROOT / "profiles" / ("yee_step_bulk_256.md" if kernel == "k_yee_step_bulk" else "yee_step_256.md")
+    name = {("k_yee_step_bulk", True): "yee_step_bulk_mat_256.md", ("k_yee_step_bulk", False): "yee_step_bulk_256.md"}
+    f = ROOT / "profiles" / name.get((kernel, mat), "yee_step_256.md")
     if not f.exists():
         return None
     for line in f.read_text().splitlines():
@@ -245,6 +247,8 @@ def run_ours(args, wl, world, rank, local):
     solver = P.Solver(prob.params)
     if tiles:
         solver.set_tiles(*tiles)
+    if args.dense_coefficients:
+        solver.use_material_index(False)
     zero = P.zero_fields(*shape)
     # Inputs resident in HBM: dense initial fields on the device, coefficients + source uploaded once.
     dev_init = [DeviceBuffer.from_array(a) for a in zero]
@@ -319,10 +323,12 @@ def run_ours(args, wl, world, rank, local):
     e2e_value = total_cell_updates / e2e_s / 1e6
     per_launch_ms = statistics.median(run_ms) / T
     peak, peak_src = hbm_peak()
-    achieved = BYTES_PER_CELL * cells / (per_launch_ms / 1e3) / 1e9
+    run_stages, mat = solver.kernel()
+    bpc = BYTES_PER_CELL_MAT if mat else BYTES_PER_CELL
+    achieved = bpc * cells / (per_launch_ms / 1e3) / 1e9
     by, kc, vec, stages = solver.tiles()
-    kernel = "k_yee_step_bulk" if stages else "k_yee_step"
-    tpc = traffic_per_cell(kernel)
+    kernel = "k_yee_step_bulk" if run_stages else "k_yee_step"
+    tpc = traffic_per_cell(kernel, mat)
     line = {
         "metric": "FDTD Mcell-updates/s", "value": value, "unit": "Mcell-updates/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
@@ -331,14 +337,19 @@ def run_ours(args, wl, world, rank, local):
         "config": {"workload": wl["desc"], "grid": list(shape), "time_steps": T,
                    "bench_step": "one complete solve (all time steps) from resident initial fields",
                    "l2": "working set %.2f GB > 129 MB L2; no flush needed" % (16 * 4 * (nx + 1) * (ny + 1) * (nz + 1) / 1e9),
-                   "tiles": {"rows": by, "z_depth": kc, "cells_per_thread": vec, "staged_planes": stages,
+                   "tiles": {"rows": by, "z_depth": kc, "cells_per_thread": vec, "staged_planes": run_stages,
                              "kernel": kernel},
+                   "coefficients": (f"material index: {solver.material_count()} distinct (Ca, Cb, Da, Db) tuples, "
+                                    "one byte per node + table; per-cell arrays given at the API" if mat else
+                                    "four per-cell FP32 arrays"),
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src,
                      "traffic": (tpc * cells) if tpc else None,
                      "kernel": kernel + " (fused H+E step)",
-                     "algorithmic_bytes_per_launch": BYTES_PER_CELL * cells,
+                     "algorithmic_bytes_per_launch": bpc * cells,
+                     "algorithmic_bytes_per_cell": bpc,
+                     "frac_of_64B_cell_traffic": BYTES_PER_CELL * cells / (per_launch_ms / 1e3) / 1e9 / peak,
                      "launch_ms": per_launch_ms},
         "e2e": {"value": e2e_value, "unit": "Mcell-updates/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3 / args.steps, "result_ok": result_ok},
@@ -437,6 +448,8 @@ def main() -> int:
     ap.add_argument("--tiles", default=None, help="fixed tile shape ROWS,DEPTH (skips the autotuner)")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--dense-coefficients", action="store_true",
+                    help="read the four per-cell coefficient arrays instead of the material index")
     ap.add_argument("--no-plain-graph", action="store_true",
                     help="batched/served: skip the per-graph (task-wise) plain dispatch arm")
     args = ap.parse_args()

@@ -130,6 +130,9 @@ struct ptk_server {
     int *d_tile0 = nullptr;
     InstDesc *h_desc = nullptr;     // pinned staging
     int *h_tile0 = nullptr;
+    long long *d_face0 = nullptr;   // staged kernel: prefix sums of the instances' face nodes
+    long long *h_face0 = nullptr;
+    long long total_faces = 0;
     int cap = 0;
     int total_tiles = 0;
     int vec = 4;                    // x cells per thread of the current work list
@@ -140,7 +143,7 @@ struct ptk_server {
     int resident = 1;               // CTAs of the step kernel that fit on the GPU at once
     int *h_err = nullptr;           // pinned copy, read after every chunk
     bool dirty = true;
-    std::map<std::tuple<int, int, int, int>, cudaGraphExec_t> graphs;
+    std::map<std::tuple<int, int, int, int, long long>, cudaGraphExec_t> graphs;
     long long chunks = 0, launches = 0;
     double wall_s = 0, cell_updates = 0;
     double t0_wall = 0;
@@ -162,14 +165,18 @@ int grow_worklist(ptk_server *s, int n)
         cudaStreamSynchronize(s->st);
         pool_free(s->d_desc, s->st);
         pool_free(s->d_tile0, s->st);
+        pool_free(s->d_face0, s->st);
         cudaFreeHost(s->h_desc);
         cudaFreeHost(s->h_tile0);
+        cudaFreeHost(s->h_face0);
     }
     int rc = pool_alloc(sizeof(InstDesc) * cap, s->st, (void **)&s->d_desc);
     if (!rc) rc = pool_alloc(sizeof(int) * (cap + 1), s->st, (void **)&s->d_tile0);
+    if (!rc) rc = pool_alloc(sizeof(long long) * (cap + 1), s->st, (void **)&s->d_face0);
     if (rc) return rc;
     PTK_CUDA_TRY(cudaMallocHost(&s->h_desc, sizeof(InstDesc) * cap));
     PTK_CUDA_TRY(cudaMallocHost(&s->h_tile0, sizeof(int) * (cap + 1)));
+    PTK_CUDA_TRY(cudaMallocHost(&s->h_face0, sizeof(long long) * (cap + 1)));
     s->cap = cap;
     for (auto &kv : s->graphs) cudaGraphExecDestroy(kv.second);
     s->graphs.clear();
@@ -232,6 +239,7 @@ InstDesc instance_desc(const ptk_server *s, const Inst *in)
         d.nmat = in->nmat;
     }
     plan_tiles(d, s->rows, instance_depth(s, in->L.nz), s->vec);
+    if (s->stages) d.face_tiles = 0;   // faces: launch_yee_faces_steps, once per chunk
     return d;
 }
 
@@ -338,17 +346,24 @@ int rebuild_worklist(ptk_server *s)
         });
     }
     int tiles = 0;
+    long long faces = 0;
     for (int q = 0; q < n; ++q) {
         const InstDesc d = instance_desc(s, s->active[q]);
         s->h_desc[q] = d;
+        s->h_face0[q] = faces;
+        faces += face_nodes(d.nx, d.ny, d.nz);
         s->h_tile0[q] = tiles;
         tiles += d.tiles_x * d.tiles_y * d.tiles_z + d.face_tiles;
     }
     s->h_tile0[n] = tiles;
     s->total_tiles = tiles;
+    s->h_face0[n] = faces;
+    s->total_faces = s->stages ? faces : 0;
     if (n) {
         PTK_CUDA_TRY(cudaMemcpyAsync(s->d_desc, s->h_desc, sizeof(InstDesc) * n, cudaMemcpyHostToDevice, s->st));
         PTK_CUDA_TRY(cudaMemcpyAsync(s->d_tile0, s->h_tile0, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s->st));
+        PTK_CUDA_TRY(cudaMemcpyAsync(s->d_face0, s->h_face0, sizeof(long long) * (n + 1), cudaMemcpyHostToDevice,
+                                     s->st));
     }
     s->dirty = false;
     return PTK_OK;
@@ -357,7 +372,7 @@ int rebuild_worklist(ptk_server *s)
 int chunk_graph(ptk_server *s, int len, int grid, cudaGraphExec_t *out)
 {
     const int n = (int)s->active.size();
-    auto key = std::make_tuple(len, n, s->total_tiles, (grid * 8 + s->vec) * 8 + s->stages);
+    auto key = std::make_tuple(len, n, s->total_tiles, (grid * 8 + s->vec) * 8 + s->stages, s->total_faces);
     auto it = s->graphs.find(key);
     if (it != s->graphs.end()) {
         *out = it->second;
@@ -372,6 +387,7 @@ int chunk_graph(ptk_server *s, int len, int grid, cudaGraphExec_t *out)
         rc = set_error(PTK_ERR_CUDA, "chunk capture: counter reset failed");
     else if (s->stages)
         count_launches(1);
+    if (!rc && s->stages) rc = launch_yee_faces_steps(s->d_desc, s->d_face0, n, s->total_faces, 0, len, cap);
     for (int q = 0; q < len && !rc; ++q)
         rc = s->stages ? launch_yee_step_bulk(s->d_desc, s->d_tile0, n, s->total_tiles, q, s->rows, s->stages, grid,
                                               s->d_err, cap, s->d_work, true)
@@ -656,8 +672,10 @@ int ptk_server_destroy(ptk_server *s)
     for (auto &kv : s->graphs) cudaGraphExecDestroy(kv.second);
     if (s->d_desc) pool_free(s->d_desc, s->st);
     if (s->d_tile0) pool_free(s->d_tile0, s->st);
+    if (s->d_face0) pool_free(s->d_face0, s->st);
     if (s->h_desc) cudaFreeHost(s->h_desc);
     if (s->h_tile0) cudaFreeHost(s->h_tile0);
+    if (s->h_face0) cudaFreeHost(s->h_face0);
     if (s->d_err) pool_free(s->d_err, s->st);
     if (s->d_work) pool_free(s->d_work, s->st);
     if (s->h_err) cudaFreeHost(s->h_err);

@@ -87,6 +87,9 @@ struct ptk_solver {
     float *mat_tab = nullptr;       // its table, kMaxMaterials x (Ca, Cb, Da, Db)
     int nmat = 0;                   // materials in the table; 0 = per-cell arrays only
     bool mat_enabled = true;
+    long long *d_face0 = nullptr;   // {0, face nodes}: the staged path advances faces per chunk
+    long long faces = 0;
+    int *d_work = nullptr;          // staged path: tile counters, one per step of a chunk
     int total_tiles = 0;
     InstDesc *d_desc = nullptr;
     int *d_tile0 = nullptr;
@@ -99,16 +102,24 @@ struct ptk_solver {
 namespace ptk {
 
 // The staged kernel reads the material index when the coefficients have one and an instantiation
-// of the shape exists; otherwise the per-cell arrays, with the ring clamped to a dense shape.
+// of the shape exists; otherwise the per-cell arrays, with the shape clamped to a dense one (the
+// 10- and 12-row and 5- and 6-stage shapes exist only with the index).
 static bool use_mat(const ptk_solver *s)
 {
     return s->stages > 0 && s->mat_enabled && s->nmat > 0 && yee_bulk_smem_bytes(s->by, s->stages, true) > 0;
 }
 
-static int run_stages(const ptk_solver *s)
+struct RunShape {
+    int by, stages;
+    bool mat;
+};
+
+static RunShape run_shape(const ptk_solver *s)
 {
-    if (s->stages <= 0 || use_mat(s) || yee_bulk_smem_bytes(s->by, s->stages, false) > 0) return s->stages;
-    return 4;
+    if (s->stages <= 0) return {s->by, 0, false};
+    if (use_mat(s)) return {s->by, s->stages, true};
+    if (yee_bulk_smem_bytes(s->by, s->stages, false) > 0) return {s->by, s->stages, false};
+    return {s->by >= 8 ? 8 : 4, 4, false};
 }
 
 static int rebuild_material(ptk_solver *s, cudaStream_t st)
@@ -133,12 +144,14 @@ static InstDesc host_desc(const ptk_solver *s, int steps_left)
     d.nwave = s->nwave;
     d.step = s->step;
     d.steps_left = steps_left;
-    if (use_mat(s)) {
+    const RunShape rs = run_shape(s);
+    if (rs.mat) {
         d.mat = s->mat;
         d.mat_tab = s->mat_tab;
         d.nmat = s->nmat;
     }
-    plan_tiles(d, s->by, s->kc, s->vec);
+    plan_tiles(d, rs.by, s->kc, s->vec);
+    if (rs.stages > 0) d.face_tiles = 0;   // faces: launch_yee_faces_steps, once per chunk
     return d;
 }
 
@@ -146,17 +159,18 @@ static int solver_sync_desc(ptk_solver *s, int steps_left, cudaStream_t st)
 {
     InstDesc d = host_desc(s, steps_left);
     s->total_tiles = d.tiles_x * d.tiles_y * d.tiles_z + d.face_tiles;
-    if (s->stages > 0) {
-        if (s->tma_by != s->by) {
+    const RunShape rs = run_shape(s);
+    if (rs.stages > 0) {
+        if (s->tma_by != rs.by) {
             // The arrays never move, so the maps change only with the tile rows.
             alignas(64) unsigned char maps[kTmaSetBytes];
             InstDesc e = d;
             e.mat = s->mat;   // the index map is always encoded; the kernel variant decides its use
-            int rc = encode_tma_set(e, s->by, maps);
+            int rc = encode_tma_set(e, rs.by, maps);
             if (rc) return rc;
             PTK_CUDA_TRY(cudaStreamSynchronize(st));
             PTK_CUDA_TRY(cudaMemcpy(s->d_tma, maps, kTmaSetBytes, cudaMemcpyHostToDevice));
-            s->tma_by = s->by;
+            s->tma_by = rs.by;
         }
         d.tma = s->d_tma;
     }
@@ -177,23 +191,32 @@ static void drop_graphs(ptk_solver *s)
 // Graph of `len` fused steps + one advance for this solver's current tile shape.
 static int solver_graph(ptk_solver *s, int len, cudaGraphExec_t *out)
 {
-    const bool mat = use_mat(s);
-    const int stages = run_stages(s);
-    GraphKey key{len, s->by, s->kc, s->vec, stages * 2 + (mat ? 1 : 0)};
+    const RunShape rs = run_shape(s);
+    GraphKey key{len, rs.by, s->kc, s->vec, rs.stages * 2 + (rs.mat ? 1 : 0)};
     auto it = s->graphs.find(key);
     if (it != s->graphs.end()) {
         *out = it->second;
         return PTK_OK;
     }
     if (!s->cap) PTK_CUDA_TRY(cudaStreamCreateWithFlags(&s->cap, cudaStreamNonBlocking));
+    // The staged kernel runs as a persistent grid of resident CTAs taking tiles from a counter, so
+    // a CTA streams several tiles through one ring and the last wave is balanced.
+    const int grid = rs.stages > 0 ? yee_bulk_resident_ctas(rs.by, rs.stages, rs.mat) : 0;
     PTK_CUDA_TRY(cudaStreamBeginCapture(s->cap, cudaStreamCaptureModeThreadLocal));
     set_capturing(true);
     int rc = PTK_OK;
+    if (rs.stages > 0) {
+        if (cudaMemsetAsync(s->d_work, 0, sizeof(int) * len, s->cap) != cudaSuccess)
+            rc = set_error(PTK_ERR_CUDA, "tile counter reset failed");
+        else
+            count_launches(1);
+    }
     for (int q = 0; q < len && rc == PTK_OK; ++q)
-        rc = stages > 0
-                 ? launch_yee_step_bulk(s->d_desc, s->d_tile0, 1, s->total_tiles, q, s->by, stages, 0, s->d_err,
-                                        s->cap, nullptr, mat)
+        rc = rs.stages > 0
+                 ? launch_yee_step_bulk(s->d_desc, s->d_tile0, 1, s->total_tiles, q, rs.by, rs.stages, grid, s->d_err,
+                                        s->cap, s->d_work, rs.mat)
                  : launch_yee_step_v(s->d_desc, s->d_tile0, 1, s->total_tiles, q, s->by, s->vec, 0, s->cap);
+    if (rc == PTK_OK && rs.stages > 0) rc = launch_yee_faces_steps(s->d_desc, s->d_face0, 1, s->faces, 0, len, s->cap);
     if (rc == PTK_OK) rc = launch_advance(s->d_desc, 1, len, s->cap);
     set_capturing(false);
     cudaGraph_t g = nullptr;
@@ -282,6 +305,14 @@ int ptk_solver_create(const ptk_fdtd_params *p, ptk_solver **out)
     if (rc == PTK_OK) rc = pool_alloc((size_t)s->L.total, st, (void **)&s->mat);
     if (rc == PTK_OK) rc = pool_alloc(sizeof(float) * 4 * kMaxMaterials, st, (void **)&s->mat_tab);
     if (rc == PTK_OK) cudaMemsetAsync(s->mat, 0, (size_t)s->L.total, st);
+    if (rc == PTK_OK) rc = pool_alloc(2 * sizeof(long long), st, (void **)&s->d_face0);
+    if (rc == PTK_OK) rc = pool_alloc(sizeof(int) * kChunk, st, (void **)&s->d_work);
+    if (rc == PTK_OK) {
+        s->faces = face_nodes(p->Nx, p->Ny, p->Nz);
+        const long long f0[2] = {0, s->faces};   // pageable: staged before the call returns
+        if (cudaMemcpyAsync(s->d_face0, f0, sizeof f0, cudaMemcpyHostToDevice, st) != cudaSuccess)
+            rc = set_error(PTK_ERR_CUDA, "face prefix upload failed");
+    }
     if (rc == PTK_OK && ((uintptr_t)s->d_tma & 63))
         rc = set_error(PTK_ERR_CUDA, "tensor-map buffer is not 64-byte aligned");
     if (rc == PTK_OK) cudaMemsetAsync(s->d_err, 0, sizeof(int), st);
@@ -322,6 +353,8 @@ int ptk_solver_destroy(ptk_solver *s)
         pool_free(s->d_tma, st);
         pool_free(s->mat, st);
         pool_free(s->mat_tab, st);
+        pool_free(s->d_face0, st);
+        pool_free(s->d_work, st);
         if (s->cap) cudaStreamDestroy(s->cap);
     }
     cudaStreamSynchronize(st);
@@ -483,7 +516,8 @@ int ptk_solver_set_tiles(ptk_solver *s, const ptk_tile_config *cfg)
     const int stages = cfg->stages;
     if (stages > 0) vec = 4;
     if (vec == 0) vec = default_vec(s->p.Nx);
-    PTK_CHECK_ARG(by == 4 || by == 8 || by == 16, "tile rows must be 4, 8 or 16 (got %d)", by);
+    PTK_CHECK_ARG(by == 4 || by == 8 || by == 16 || (stages > 0 && (by == 10 || by == 11)),
+                  "tile rows must be 4, 8 or 16, or 10 or 11 with a staged ring (got %d)", by);
     PTK_CHECK_ARG(vec == 1 || vec == 2 || vec == 4, "cells per thread must be 1, 2 or 4 (got %d)", vec);
     PTK_CHECK_ARG(stages == 0 || yee_bulk_smem_bytes(by, stages, false) > 0 || yee_bulk_smem_bytes(by, stages, true) > 0,
                   "no staged kernel for %d rows with %d stages", by, stages);
@@ -515,8 +549,9 @@ int ptk_solver_material_count(const ptk_solver *s, int *nmat)
 int ptk_solver_kernel(const ptk_solver *s, int *stages, int *material_index)
 {
     PTK_CHECK_ARG(s && stages && material_index, "NULL argument");
-    *stages = run_stages(s);
-    *material_index = use_mat(s) ? 1 : 0;
+    const RunShape rs = run_shape(s);
+    *stages = rs.stages;
+    *material_index = rs.mat ? 1 : 0;
     return PTK_OK;
 }
 
@@ -670,7 +705,8 @@ int ptk_autotune_tiles(int Nx, int Ny, int Nz, ptk_tile_config *best, float *bes
             add(by, vec, 0, yee_resident_ctas(by, vec));
         }
     // Staged shapes: timed on vacuum coefficients, i.e. with the material index where the shape has it.
-    const int staged[10][2] = {{4, 2}, {4, 3}, {4, 4}, {4, 5}, {4, 6}, {8, 2}, {8, 3}, {8, 4}, {8, 5}, {8, 6}};
+    const int staged[13][2] = {{4, 2}, {4, 3}, {4, 4}, {4, 5}, {4, 6}, {8, 2}, {8, 3}, {8, 4}, {8, 5}, {8, 6},
+                               {10, 4}, {10, 5}, {11, 4}};
     for (const auto &bs : staged) {
         const bool m = yee_bulk_smem_bytes(bs[0], bs[1], true) > 0;
         add(bs[0], 4, bs[1], yee_bulk_resident_ctas(bs[0], bs[1], m));

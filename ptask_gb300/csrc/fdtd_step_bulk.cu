@@ -179,6 +179,47 @@ __device__ __forceinline__ const unsigned char *row_mat(const unsigned char *st,
 
 }  // namespace
 
+// One main tile of an instance: where it lies and the z-planes it streams (kstart .. k1; plane
+// kstart is the warm plane when k0 > 0, plane k1 is read as "next" only).
+struct Tile {
+    const InstDesc *D;
+    const CUtensorMap *maps;
+    int par, x0, y0, k0, k1, kstart, nplanes;
+};
+
+// Tile t of the concatenated main-tile lists; false when its instance has no step left.
+template <int BY>
+__device__ __forceinline__ bool tile_at(int t, const InstDesc *__restrict__ insts, const int *__restrict__ tile0,
+                                        int ninst, int s_off, Tile &T)
+{
+    int lo = 0, hi = ninst;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(tile0 + mid) <= t) lo = mid; else hi = mid;
+    }
+    const InstDesc *D = insts + lo;
+    if (s_off >= D->steps_left) return false;
+    int r0 = t - __ldg(tile0 + lo);
+    const int xt = r0 % D->tiles_x;
+    r0 /= D->tiles_x;
+    const int yt = r0 % D->tiles_y;
+    const int zt = r0 / D->tiles_y;
+    T.D = D;
+    T.maps = reinterpret_cast<const CUtensorMap *>(D->tma);
+    T.par = (D->step + s_off) & 1;
+    T.x0 = xt * 128;
+    T.y0 = yt * BY;
+    T.k0 = zt * D->kc;
+    T.k1 = min(T.k0 + D->kc, D->nz);
+    T.kstart = T.k0 > 0 ? T.k0 - 1 : T.k0;
+    T.nplanes = T.k1 - T.kstart + 1;
+    return true;
+}
+
+// The tile lists hold main tiles only: the H nodes of the i = Nx, j = Ny, k = Nz faces are advanced
+// by k_yee_faces_steps.  A CTA streams its tiles' planes through one continuous ring: it knows its
+// next tile while it works on the current one, and once the current tile's planes are all in
+// flight the refills continue with the next tile's, so a tile starts without a pipeline fill.
 template <int BY, int S, bool MAT>
 __global__ void __launch_bounds__(32 * (BY + 1), 1)
 k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile0, int ninst, int s_off,
@@ -204,12 +245,9 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
     }
     __syncthreads();
 
-    unsigned gbase = 0;     // planes loaded by this CTA before the current tile
-    bool failed = false;
-
     // Tiles: the first one is blockIdx.x; later ones are static (t + gridDim.x) or, with a work
-    // counter (zeroed before the launch), taken in list order as CTAs free up.  Every branch that
-    // ends a tile is uniform across the CTA, so the barriers in `advance` are reached by all.
+    // counter (zeroed before the launch), taken in list order as CTAs free up.  All threads take
+    // every branch below together, so the barriers in `advance` are reached by all.
     auto advance = [&](int t) -> int {
         if (!work) return t + (int)gridDim.x;
         __syncthreads();
@@ -217,27 +255,55 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
         __syncthreads();
         return *slot;
     };
-    for (int t = blockIdx.x; t < total_tiles; t = advance(t)) {
-        int lo = 0, hi = ninst;
-        while (hi - lo > 1) {
-            const int mid = (lo + hi) >> 1;
-            if (__ldg(tile0 + mid) <= t) lo = mid; else hi = mid;
+    auto fetch = [&](int &t, Tile &T) -> bool {   // first live tile at or after t
+        while (t < total_tiles) {
+            if (tile_at<BY>(t, insts, tile0, ninst, s_off, T)) return true;
+            t = advance(t);
         }
-        const InstDesc *__restrict__ D = insts + lo;
-        if (s_off >= D->steps_left) continue;
-        const int lt = t - __ldg(tile0 + lo);
-        const int step = D->step + s_off;
-        const int par = step & 1;
-        const int nmain = D->tiles_x * D->tiles_y * D->tiles_z;
-        if (lt >= nmain) {
-            yee_faces(D, par, lt - nmain, 32 * (BY + 1) * kFaceCellsPerThread);
-            continue;
-        }
+        return false;
+    };
 
-        const int nx = D->nx, ny = D->ny, nz = D->nz, pitch = D->pitch, kc = D->kc;
-        const long long plane = D->plane;
-        const float cx = D->cx, cy = D->cy, cz = D->cz;
-        const CUtensorMap *maps = reinterpret_cast<const CUtensorMap *>(D->tma);
+    int t = blockIdx.x, t1 = total_tiles;
+    Tile T0{}, T1{};
+    bool have0 = fetch(t, T0), have1 = false;
+    if (have0) {
+        t1 = advance(t);
+        have1 = fetch(t1, T1);
+    }
+    // Ring positions: the planes of this CTA's tiles in order; plane j of the current tile is
+    // position gbase + j.  Positions below `issued` are in flight or consumed.
+    unsigned gbase = 0, issued = 0;
+    bool acq0 = false, acq1 = false;   // tensor maps of T0 / T1 acquire-fenced by warp 0
+    bool failed = false;
+    // Issue every position below `limit` that belongs to the current or the next tile (warp 0).
+    auto top_up = [&](unsigned limit) {
+        while (issued < limit) {
+            const unsigned p = issued;
+            if (p < gbase + (unsigned)T0.nplanes) {
+                if (!acq0) {
+                    if (lane < n_arrays<MAT>()) tma_acquire(map_of<MAT>(T0.maps, lane, T0.par));
+                    acq0 = true;
+                }
+                const int j = (int)(p - gbase);
+                issue_plane<BY, MAT>(T0.maps, T0.par, T0.x0, T0.y0, T0.kstart + j, T0.kstart + j == T0.k1,
+                                     stages + (size_t)(p % S) * SB, &bars[p % S], lane);
+            } else if (have1 && p < gbase + (unsigned)(T0.nplanes + T1.nplanes)) {
+                if (!acq1) {
+                    if (lane < n_arrays<MAT>()) tma_acquire(map_of<MAT>(T1.maps, lane, T1.par));
+                    acq1 = true;
+                }
+                const int j = (int)(p - gbase) - T0.nplanes;
+                issue_plane<BY, MAT>(T1.maps, T1.par, T1.x0, T1.y0, T1.kstart + j, T1.kstart + j == T1.k1,
+                                     stages + (size_t)(p % S) * SB, &bars[p % S], lane);
+            } else {
+                break;
+            }
+            ++issued;
+        }
+    };
+
+    while (have0) {
+        const InstDesc *__restrict__ D = T0.D;
         if constexpr (MAT) {
             // The previous tile ended with a block barrier: nobody reads the old table any more.
             if (D->mat_tab != tab_src) {
@@ -247,6 +313,13 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
                 __syncthreads();
             }
         }
+        if (ty == 0) top_up(gbase + S);
+
+        const int nx = D->nx, ny = D->ny, pitch = D->pitch;
+        const long long plane = D->plane;
+        const float cx = D->cx, cy = D->cy, cz = D->cz;
+        const int par = T0.par, x0 = T0.x0, y0 = T0.y0, k0 = T0.k0, k1 = T0.k1, kstart = T0.kstart;
+        const int step = D->step + s_off;
         float *__restrict__ oHx = D->buf[par ^ 1][0];
         float *__restrict__ oHy = D->buf[par ^ 1][1];
         float *__restrict__ oHz = D->buf[par ^ 1][2];
@@ -255,25 +328,6 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
         float *__restrict__ oEz = D->buf[par ^ 1][5];
         const long long src = D->src;
         const float srcv = (src >= 0 && step < D->nwave) ? __ldg(D->wave + step) : 0.f;
-
-        int r0 = lt;
-        const int xt = r0 % D->tiles_x; r0 /= D->tiles_x;
-        const int yt = r0 % D->tiles_y;
-        const int zt = r0 / D->tiles_y;
-        const int x0 = xt * 128, y0 = yt * BY;
-        const int k0 = zt * kc, k1 = min(k0 + kc, nz);
-        const int kstart = k0 > 0 ? k0 - 1 : k0;
-        const int nplanes = k1 - kstart + 1;   // planes kstart..k1 (k1 is read as "next" only)
-
-        // prologue: the first S planes
-        if (ty == 0) {
-            if (lane < n_arrays<MAT>()) tma_acquire(map_of<MAT>(maps, lane, par));
-            for (int q = 0; q < S && q < nplanes; ++q) {
-                const unsigned G = gbase + q;
-                issue_plane<BY, MAT>(maps, par, x0, y0, kstart + q, kstart + q == k1, stages + (size_t)(G % S) * SB,
-                                     &bars[G % S], lane);
-            }
-        }
 
         const int i = x0 + 4 * lane;
         const int r = ty;                 // frame row of this thread
@@ -385,12 +439,9 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
             }
             __syncthreads();
             // Plane k's stage was read (as "next") before the previous barrier and (as "current")
-            // before this one, and nothing after this barrier reads a stage: refill it now.
-            if (ty == 0 && q + S < nplanes) {
-                const unsigned G = gbase + q + S;
-                issue_plane<BY, MAT>(maps, par, x0, y0, kstart + q + S, kstart + q + S == k1, stages + (size_t)(G % S) * SB,
-                                     &bars[G % S], lane);
-            }
+            // before this one, and nothing after this barrier reads a stage: refill it now (with a
+            // plane of the next tile once this tile's planes are all in flight).
+            if (ty == 0) top_up(gbase + q + 1 + S);
             float hy_p = __shfl_up_sync(0xffffffffu, hyn[3], 1);
             float hz_p = __shfl_up_sync(0xffffffffu, hzn[3], 1);
             if (lane == 0) { hy_p = hyh; hz_p = hzh; }
@@ -438,16 +489,93 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
                 hyp = make_float4(hyn[0], hyn[1], hyn[2], hyn[3]);
             }
         }
-        gbase += (unsigned)nplanes;
-        // The last plane's stage buffers are refilled by the next tile only after its first
-        // barrier, which every thread reaches after finishing this tile.
+        gbase += (unsigned)T0.nplanes;
+        // The stages of this tile are refilled only after the barriers of the planes that follow
+        // them, which every thread reaches after finishing this tile.
         __syncthreads();
+        T0 = T1;
+        have0 = have1;
+        acq0 = acq1;
+        acq1 = false;
+        have1 = false;
+        if (have0) {
+            t = t1;
+            t1 = advance(t);
+            have1 = fetch(t1, T1);
+        }
     }
     // Every issued plane has normally been waited for.  If a wait expired, let the copies still
     // in flight land (bounded) before this CTA's shared memory is released.
     if (ty == 0 && lane == 0)
-        for (unsigned G = gbase > (unsigned)S ? gbase - S : 0u; G < gbase; ++G) mbar_wait(&bars[G % S], (G / S) & 1);
+        for (unsigned G = issued > (unsigned)S ? issued - S : 0u; G < issued; ++G) mbar_wait(&bars[G % S], (G / S) & 1);
 }
+
+// The H nodes outside the cell block (Hx at i = Nx, Hy at j = Ny, Hz at k = Nz) for `len` steps
+// from step offset s_off.  Their update reads only E nodes on the PEC walls, which never change,
+// and no other node's update reads them, so each evolves alone: H <- Da*H + Db*curl with a fixed
+// curl, the same operations in the same order as one step at a time.  Thread per face node over
+// all instances (face0: prefix of the instances' face-node counts); the result is written to the
+// buffer of the parity the instance's step counter has after its steps in this range.
+__global__ void k_yee_faces_steps(const InstDesc *__restrict__ insts, const long long *__restrict__ face0,
+                                  int ninst, int s_off, int len)
+{
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= __ldg(face0 + ninst)) return;
+    int lo = 0, hi = ninst;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(face0 + mid) <= g) lo = mid; else hi = mid;
+    }
+    const InstDesc *__restrict__ D = insts + lo;
+    const int n = min(len, D->steps_left - s_off);
+    if (n <= 0) return;
+    const int nx = D->nx, ny = D->ny, nz = D->nz, pitch = D->pitch;
+    const long long plane = D->plane;
+    const int p0 = (D->step + s_off) & 1;
+    const float *__restrict__ Ex = D->buf[p0][3];
+    const float *__restrict__ Ey = D->buf[p0][4];
+    const float *__restrict__ Ez = D->buf[p0][5];
+    const long long A = (long long)ny * nz, B = (long long)nx * nz;
+    const long long q = g - __ldg(face0 + lo);
+    long long o;
+    int f;
+    float a1, a0, s1, b1, b0, s2;
+    if (q < A) {                       // Hx at i = Nx: (Ey(k+1) - Ey(k)) Cz - (Ez(j+1) - Ez(j)) Cy
+        const int j = (int)(q % ny), k = (int)(q / ny);
+        o = nx + (long long)pitch * j + plane * k;
+        f = 0;
+        a1 = Ey[o + plane]; a0 = Ey[o]; s1 = D->cz; b1 = Ez[o + pitch]; b0 = Ez[o]; s2 = D->cy;
+    } else if (q < A + B) {            // Hy at j = Ny: (Ez(i+1) - Ez(i)) Cx - (Ex(k+1) - Ex(k)) Cz
+        const long long r = q - A;
+        const int i = (int)(r % nx), k = (int)(r / nx);
+        o = i + (long long)pitch * ny + plane * k;
+        f = 1;
+        a1 = Ez[o + 1]; a0 = Ez[o]; s1 = D->cx; b1 = Ex[o + plane]; b0 = Ex[o]; s2 = D->cz;
+    } else {                           // Hz at k = Nz: (Ex(j+1) - Ex(j)) Cy - (Ey(i+1) - Ey(i)) Cx
+        const long long r = q - A - B;
+        const int i = (int)(r % nx), j = (int)(r / nx);
+        o = i + (long long)pitch * j + plane * nz;
+        f = 2;
+        a1 = Ex[o + pitch]; a0 = Ex[o]; s1 = D->cy; b1 = Ey[o + 1]; b0 = Ey[o]; s2 = D->cx;
+    }
+    const float da = D->coef[2][o], db = D->coef[3][o];
+    float h = D->buf[p0][f][o];
+    for (int s = 0; s < n; ++s) h = yee_b(da, h, db, a1, a0, s1, b1, b0, s2);
+    D->buf[(p0 + n) & 1][f][o] = h;
+}
+
+int launch_yee_faces_steps(const InstDesc *d_insts, const long long *d_face0, int ninst, long long total_faces,
+                           int s_offset, int len, cudaStream_t s)
+{
+    if (total_faces <= 0 || len <= 0) return PTK_OK;
+    const long long blocks = (total_faces + 255) / 256;
+    k_yee_faces_steps<<<(unsigned)blocks, 256, 0, s>>>(d_insts, d_face0, ninst, s_offset, len);
+    PTK_CUDA_TRY(cudaGetLastError());
+    count_launches(1);
+    return PTK_OK;
+}
+
+long long face_nodes(int nx, int ny, int nz) { return (long long)ny * nz + (long long)nx * nz + (long long)nx * ny; }
 
 // Opt the instantiation into its dynamic shared memory (once per process; repeating it is harmless).
 template <int BY, int S, bool MAT>
@@ -457,6 +585,9 @@ static int prepare_bulk()
     if (!attr_set) {
         PTK_CUDA_TRY(cudaFuncSetAttribute(k_yee_step_bulk<BY, S, MAT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)smem_bytes<BY, S, MAT>()));
+        // all of the unified L1 / shared storage as shared memory, so small rings can co-reside
+        PTK_CUDA_TRY(cudaFuncSetAttribute(k_yee_step_bulk<BY, S, MAT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                          100));
         attr_set = true;
     }
     return PTK_OK;
@@ -494,7 +625,8 @@ static int launch_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, i
 #define PTK_DENSE_SHAPES(X) X(4, 2, false) X(4, 3, false) X(4, 4, false) X(4, 5, false) \
     X(8, 2, false) X(8, 3, false) X(8, 4, false)
 #define PTK_MAT_SHAPES(X) X(4, 2, true) X(4, 3, true) X(4, 4, true) X(4, 5, true) X(4, 6, true) \
-    X(8, 2, true) X(8, 3, true) X(8, 4, true) X(8, 5, true) X(8, 6, true)
+    X(8, 2, true) X(8, 3, true) X(8, 4, true) X(8, 5, true) X(8, 6, true) \
+    X(10, 4, true) X(10, 5, true) X(11, 4, true)
 
 int launch_yee_step_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles, int s_offset,
                          int by, int stages, int grid, int *err, cudaStream_t s, int *work, bool mat)
@@ -574,6 +706,8 @@ int encode_tma_set(const InstDesc &d, int by, void *host_out)
     CUtensorMap *out = static_cast<CUtensorMap *>(host_out);
     if (by == 4) return encode_set<4>(d, out);
     if (by == 8) return encode_set<8>(d, out);
+    if (by == 10) return encode_set<10>(d, out);
+    if (by == 11) return encode_set<11>(d, out);
     return set_error(PTK_ERR_INVALID, "no staged kernel for %d rows", by);
 }
 

@@ -122,6 +122,12 @@ int launch_yee_step_v(const InstDesc *d_insts, const int *d_tile0, int ninst, in
 int launch_yee_step_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles, int s_offset,
                          int by, int stages, int grid, int *err, cudaStream_t s, int *work = nullptr,
                          bool mat = false);
+// The face H nodes (Hx at i = Nx, Hy at j = Ny, Hz at k = Nz) of every instance advanced by `len`
+// steps from step offset s_offset in one launch; the staged kernel's tile lists leave them out
+// (descriptors planned with face_tiles = 0).  d_face0: ninst + 1 prefix sums of face_nodes().
+int launch_yee_faces_steps(const InstDesc *d_insts, const long long *d_face0, int ninst, long long total_faces,
+                           int s_offset, int len, cudaStream_t s);
+long long face_nodes(int nx, int ny, int nz);
 // Shared memory of a staged instantiation (0: no such kernel).
 size_t yee_bulk_smem_bytes(int by, int stages, bool mat = false);
 // CTAs of the staged kernel that fit on the whole GPU at once (0: no such kernel).
