@@ -250,7 +250,8 @@ typedef struct ptk_server_config {
     size_t hbm_budget_bytes;   /* device bytes the admitted instances may hold (0: 80% of free HBM) */
     int max_active;            /* instance slots (0: unlimited; 1: plain one-at-a-time dispatch) */
     int chunk_steps;           /* steps per replayed graph between admission points (0: 32) */
-    int tile_rows;             /* fused-kernel tile rows 4, 8 or 16 (0: 8) */
+    int tile_rows;             /* fused-kernel tile rows 4, 8 or 16, or 10 or 11 with the staged kernel
+                                  (0: 11 for the staged kernel, 8 for the register kernel) */
     int keep_results;          /* keep finished fields for ptk_server_fetch */
     int persistent;            /* persistent grid of resident CTAs instead of one CTA per tile */
     int stages;                /* step kernel: 0 = TMA-staged with its default ring (tile_rows 4 or 8,

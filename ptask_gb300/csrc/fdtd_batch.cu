@@ -456,7 +456,10 @@ int ptk_server_create(const ptk_server_config *cfg, ptk_server **out)
     s->cfg = *cfg;
     if (s->cfg.max_active <= 0) s->cfg.max_active = 1 << 20;
     if (s->cfg.chunk_steps <= 0) s->cfg.chunk_steps = 32;
-    if (s->cfg.tile_rows != 4 && s->cfg.tile_rows != 8 && s->cfg.tile_rows != 16) s->cfg.tile_rows = 8;
+    // default rows: 11 for the staged kernel (twelve warps per CTA; measured best), 8 otherwise
+    if (s->cfg.tile_rows == 0) s->cfg.tile_rows = s->cfg.stages >= 0 ? 11 : 8;
+    const bool staged_rows = s->cfg.stages >= 0 && (s->cfg.tile_rows == 10 || s->cfg.tile_rows == 11);
+    if (s->cfg.tile_rows != 4 && s->cfg.tile_rows != 8 && s->cfg.tile_rows != 16 && !staged_rows) s->cfg.tile_rows = 8;
     s->rows = s->cfg.tile_rows;
     if (s->cfg.stages < 0) {
         s->stages = 0;

@@ -61,6 +61,13 @@ __device__ void insert(MatScratch *S, uint4 key)
 {
     unsigned h = mix(key) & (kSlots - 1);
     for (int probe = 0; probe < kSlots; ++probe, h = (h + 1) & (kSlots - 1)) {
+        // Most nodes repeat a tuple that is already published: check with a plain read first, so
+        // that only new tuples contend for a slot with an atomic.
+        if (reinterpret_cast<volatile unsigned *>(S->state)[h] == 2u) {
+            __threadfence();
+            if (same(read_key(S, h), key)) return;
+            continue;
+        }
         const unsigned st = atomicCAS(&S->state[h], 0u, 1u);
         if (st == 0u) {
             S->key[h] = key;

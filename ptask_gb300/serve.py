@@ -64,7 +64,7 @@ def poisson_trace(n: int, rate: float, seed: int = 5, edge=(24, 256), steps=(50,
 class Server:
     """Continuous-batching FDTD server (max_active=1 gives plain one-at-a-time dispatch)."""
 
-    def __init__(self, budget_bytes: int = 0, max_active: int = 0, chunk_steps: int = 32, tile_rows: int = 8,
+    def __init__(self, budget_bytes: int = 0, max_active: int = 0, chunk_steps: int = 32, tile_rows: int = 0,
                  keep_results: bool = False, persistent: bool = True, stages: int = 0):
         """`stages`: 0 = TMA-staged step kernel with its default ring, 2..5 = that many planes,
         -1 = register kernel."""

@@ -17,7 +17,7 @@ def alone(r: Request):
     return P.solve(pr, P.zero_fields(r.nx, r.ny, r.nz), r.steps), pr
 
 
-@pytest.mark.parametrize("rows,stages", [(8, 0), (8, -1), (4, 3), (8, 2)])
+@pytest.mark.parametrize("rows,stages", [(0, 0), (8, 0), (8, -1), (4, 3), (8, 2), (10, 5)])
 def test_mixed_batch_results_equal_alone(rows, stages):
     """Staged (default ring, 2-plane ring, 4 rows) and register kernels all give the solo results."""
     reqs = [Request(24, 20, 16, 40, 2, 1), Request(37, 29, 23, 75, 3, 2), Request(64, 48, 40, 33, 1, 3),
