@@ -300,14 +300,28 @@ def run_ours(args, wl, world, rank, local):
     h2d = sum(a.nbytes for a in zero) + 4 * prob.Ca.nbytes + prob.wave.nbytes
     d2h = sum(a.nbytes for a in zero)
 
-    def e2e_step():
+    phase_ev = [Event() for _ in range(4)]
+    phase_ms = {"upload": 0.0, "solve": 0.0, "download": 0.0}
+
+    def e2e_step(record=False):
+        if record:
+            phase_ev[0].record()
         _lib.call("ptk_solver_set_fields", solver.handle, in_ptrs, _lib.PTK_HOST, None)
         _lib.call("ptk_solver_set_coefficients", solver.handle, *[h.ptr.value for h in hcoef], _lib.PTK_HOST, None)
         _lib.call("ptk_solver_set_source", solver.handle, *prob.src, hwave.ptr.value, prob.wave.size,
                   _lib.PTK_HOST, None)
         solver.reset_clock()
+        if record:
+            phase_ev[1].record()
         solver.run(T)
+        if record:
+            phase_ev[2].record()
         _lib.call("ptk_solver_get_fields", solver.handle, out_ptrs, _lib.PTK_HOST, None)
+        if record:
+            phase_ev[3].record()
+            phase_ev[3].sync()
+            for name, a, b in (("upload", 0, 1), ("solve", 1, 2), ("download", 2, 3)):
+                phase_ms[name] += phase_ev[a].elapsed_ms(phase_ev[b])
 
     for _ in range(max(1, args.warmup)):
         e2e_step()
@@ -316,6 +330,9 @@ def run_ours(args, wl, world, rank, local):
     for _ in range(args.steps):
         e2e_step()
     e2e_s = dist.max(time.perf_counter() - t0)
+    # the same steps again with device events between the phases (not part of the timed value)
+    for _ in range(args.steps):
+        e2e_step(record=True)
     result_ok = bool(np.isfinite(hout[5].array).all() and np.abs(hout[5].array).max() > 0)
 
     total_cell_updates = cells * T * args.steps * world
@@ -352,7 +369,8 @@ def run_ours(args, wl, world, rank, local):
                      "frac_of_64B_cell_traffic": BYTES_PER_CELL * cells / (per_launch_ms / 1e3) / 1e9 / peak,
                      "launch_ms": per_launch_ms},
         "e2e": {"value": e2e_value, "unit": "Mcell-updates/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3 / args.steps, "result_ok": result_ok},
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3 / args.steps, "result_ok": result_ok,
+                "phases_ms_per_step": {k: v / args.steps for k, v in phase_ms.items()}},
         "gpu_launches": int(launches),
         "clocks": clk,
     }

@@ -496,8 +496,10 @@ int ptk_solver_reset_clock(ptk_solver *s, void *stream)
     // The parity of the current field buffer is tied to the step counter; keep it and only
     // rebase the waveform index by storing the offset in the host mirror.
     if (s->step & 1) {
-        // Swap buffer roles so that step 0 reads the buffer that holds the current fields.
+        // Swap buffer roles so that step 0 reads the buffer that holds the current fields.  The
+        // staged kernel's tensor maps name the buffers by parity: encode them again.
         for (int f = 0; f < 6; ++f) std::swap(s->buf[0][f], s->buf[1][f]);
+        s->tma_by = 0;
     }
     s->step = 0;
     return PTK_OK;

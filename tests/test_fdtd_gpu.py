@@ -159,6 +159,26 @@ def test_run_split_and_chunking_is_invisible():
             np.testing.assert_array_equal(a, b)
 
 
+@pytest.mark.parametrize("tiles", [(11, 5, 4, 4), (8, 0, 4, 0)])
+def test_reset_clock_after_odd_steps(tiles):
+    """reset_clock after an odd step count swaps the buffer roles; the next run (staged kernel
+    tensor maps included) must continue from the current fields.  No source, so the clock
+    restart does not change the result: run(3) + reset + run(4) == run(7)."""
+    shape = (150, 37, 21)
+    pr = P.Problem.generate(*shape, n_boxes=3, eps=(1, 10), box=(5, 30), steps=7, seed=16)
+    pr = P.Problem(pr.params, pr.Ca, pr.Cb, pr.Da, pr.Db, (-1, -1, -1), np.zeros(0, np.float32))
+    f = P.random_fields(*shape, seed=75, scale=1e-2)
+    ref = oracle.step_ext_f32(f, 7, pr.params, pr.Ca, pr.Cb, pr.Da, pr.Db)
+    with P.Solver(pr.params) as s:
+        s.set_tiles(*tiles)
+        s.set_fields(f)
+        s.set_problem(pr)
+        s.run(3)
+        s.reset_clock()
+        s.run(4)
+        assert_parity(s.get_fields(), ref, f"reset_clock {tiles}")
+
+
 def test_one_call_solve_with_host_buffers():
     shape, steps = (24, 20, 16), 30
     pr = P.Problem.generate(*shape, n_boxes=2, steps=steps, seed=9)
