@@ -102,8 +102,9 @@ struct ptk_solver {
 namespace ptk {
 
 // The staged kernel reads the material index when the coefficients have one and an instantiation
-// of the shape exists; otherwise the per-cell arrays, with the shape clamped to a dense one (the
-// 10- and 12-row and 5- and 6-stage shapes exist only with the index).
+// of the shape exists; otherwise the per-cell arrays, with the shape clamped to a dense one (10- and
+// 11-row tiles have only a 3-plane ring with the per-cell arrays; 5 and 6 planes exist only with
+// the index).
 static bool use_mat(const ptk_solver *s)
 {
     return s->stages > 0 && s->mat_enabled && s->nmat > 0 && yee_bulk_smem_bytes(s->by, s->stages, true) > 0;
@@ -119,6 +120,8 @@ static RunShape run_shape(const ptk_solver *s)
     if (s->stages <= 0) return {s->by, 0, false};
     if (use_mat(s)) return {s->by, s->stages, true};
     if (yee_bulk_smem_bytes(s->by, s->stages, false) > 0) return {s->by, s->stages, false};
+    // same rows with the 3-plane ring the per-cell arrays leave room for (10 and 11 rows), else 4
+    if (yee_bulk_smem_bytes(s->by, 3, false) > 0) return {s->by, 3, false};
     return {s->by >= 8 ? 8 : 4, 4, false};
 }
 

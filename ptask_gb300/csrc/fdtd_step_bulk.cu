@@ -623,7 +623,7 @@ static int launch_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, i
 // of plane q+1 before its barrier, and the stage of plane q+1 is issued after the barrier of plane
 // q+1-S, so q+1-S <= q-1.  The material-index stages are smaller, so deeper rings fit.
 #define PTK_DENSE_SHAPES(X) X(4, 2, false) X(4, 3, false) X(4, 4, false) X(4, 5, false) \
-    X(8, 2, false) X(8, 3, false) X(8, 4, false)
+    X(8, 2, false) X(8, 3, false) X(8, 4, false) X(10, 3, false) X(11, 3, false)
 #define PTK_MAT_SHAPES(X) X(4, 2, true) X(4, 3, true) X(4, 4, true) X(4, 5, true) X(4, 6, true) \
     X(8, 2, true) X(8, 3, true) X(8, 4, true) X(8, 5, true) X(8, 6, true) \
     X(10, 4, true) X(10, 5, true) X(11, 4, true)

@@ -326,7 +326,7 @@ def test_staged_kernel_small_and_edge_shapes(shape):
 # ------------------------------------------------------------------------------------------------
 # Material index: one byte per node + a table instead of the four coefficient arrays.
 # ------------------------------------------------------------------------------------------------
-@pytest.mark.parametrize("by,stages", [(8, 4), (8, 6), (4, 3), (4, 5), (8, 2), (10, 4), (10, 5)])
+@pytest.mark.parametrize("by,stages", [(8, 4), (8, 6), (4, 3), (4, 5), (8, 2), (10, 4), (10, 5), (11, 4)])
 def test_material_index_equals_per_cell_arrays(by, stages):
     shape, steps = (261, 37, 23), 7
     pr = P.Problem.generate(*shape, n_boxes=5, eps=(1, 10), box=(5, 30), steps=steps, seed=15)
@@ -340,8 +340,9 @@ def test_material_index_equals_per_cell_arrays(by, stages):
             s.use_material_index(use)
             assert (s.material_count() > 0) == use and s.material_count() <= 6
             st, mat = s.kernel()
-            dense_shape = by in (4, 8) and stages <= (5 if by == 4 else 4)   # per-cell-array instantiations
-            assert mat == use and st == (stages if (use or dense_shape) else 4)
+            dense = {4: (2, 3, 4, 5), 8: (2, 3, 4), 10: (3,), 11: (3,)}   # per-cell-array instantiations
+            fallback = stages if stages in dense[by] else (3 if 3 in dense[by] else 4)
+            assert mat == use and st == (stages if use else fallback)
             s.set_fields(f)
             s.run(steps)
             outs.append(s.get_fields())
