@@ -406,7 +406,7 @@ def run_served(args, kind, world, rank, local):
     cells = sum(r.cell_updates for r in reqs)
 
     def serve(max_active):
-        with Server(max_active=max_active, chunk_steps=32, persistent=True) as s:
+        with Server(max_active=max_active, chunk_steps=32, persistent=True, tile_rows=args.server_rows) as s:
             for r in reqs:
                 s.submit(r)
             l0 = P.launch_count()
@@ -435,6 +435,8 @@ def run_served(args, kind, world, rank, local):
         "mcell_updates_per_s": cells / wall / 1e6,
         "p50_latency_s": best["p50_latency_s"], "p99_latency_s": best["p99_latency_s"],
         "peak_active": best["peak_active"], "peak_bytes": best["peak_bytes"],
+        "wall_breakdown_s": {k: best[k] for k in ("wall_s", "chunk_device_s", "admit_s", "retire_s", "schedule_s")},
+        "chunks": best["chunks"], "graph_captures": best["graph_captures"],
         "plain": {"solves_per_s": len(reqs) / plain["wall_s"], "mcell_updates_per_s": cells / plain["wall_s"] / 1e6,
                   "p50_latency_s": plain["p50_latency_s"], "p99_latency_s": plain["p99_latency_s"],
                   "wall_s": plain["wall_s"]},
@@ -463,6 +465,8 @@ def main() -> int:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batched", "served"], default="plain256")
     ap.add_argument("--requests", type=int, default=1000, help="served workload: requests in the trace")
+    ap.add_argument("--server-rows", type=int, default=0,
+                    help="batched / served: staged tile rows (0: the server's default; 23: 64-wide tiles)")
     ap.add_argument("--tiles", default=None, help="fixed tile shape ROWS,DEPTH (skips the autotuner)")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")

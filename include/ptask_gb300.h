@@ -163,9 +163,10 @@ typedef struct ptk_solver ptk_solver;
 /* Tile shape of the fused step kernel.  by: rows per CTA (4, 8 or 16); kc: z-planes per CTA (>=1,
  * 0 = whole depth); vec: x cells per thread (1, 2 or 4; tiles are 32*vec cells wide, 0 = choose
  * from Nx); stages: 0 = operands loaded into registers, 2..6 = operands staged into shared memory
- * by TMA tensor copies with that many z-planes in the ring (needs vec 4 and by 4 or 8; 5 and 6
- * stages only with the material index, see ptk_solver_use_material_index).
- * by = kc = 0 selects the default shape. */
+ * by TMA tensor copies with that many z-planes in the ring.  Staged tiles are 128 cells wide with
+ * by 4, 8, 10 or 11 and 64 cells wide with by 7 (four-warp CTAs, three per SM) or 23 (vec is set
+ * to match); 7, 10, 11 and 23 rows, and 5 and 6 stages, exist only with the material index
+ * (ptk_solver_use_material_index) except 10 and 11 rows with 3 stages.  by = kc = 0 selects the default shape. */
 typedef struct ptk_tile_config {
     int by;
     int kc;
@@ -250,12 +251,14 @@ typedef struct ptk_server_config {
     size_t hbm_budget_bytes;   /* device bytes the admitted instances may hold (0: 80% of free HBM) */
     int max_active;            /* instance slots (0: unlimited; 1: plain one-at-a-time dispatch) */
     int chunk_steps;           /* steps per replayed graph between admission points (0: 32) */
-    int tile_rows;             /* fused-kernel tile rows 4, 8 or 16, or 10 or 11 with the staged kernel
-                                  (0: 11 for the staged kernel, 8 for the register kernel) */
+    int tile_rows;             /* fused-kernel tile rows 4, 8 or 16, or 7, 10, 11 or 23 with the
+                                  staged kernel (7- and 23-row tiles are 64 cells wide, the others
+                                  128; 0: 11 for the staged kernel, 8 for the register kernel) */
     int keep_results;          /* keep finished fields for ptk_server_fetch */
     int persistent;            /* persistent grid of resident CTAs instead of one CTA per tile */
-    int stages;                /* step kernel: 0 = TMA-staged with its default ring (tile_rows 4 or 8,
-                                  else 8), 2..5 = TMA-staged with that many planes, -1 = register kernel */
+    int stages;                /* step kernel: 0 = TMA-staged with its default ring (3 planes for 4 rows,
+                                  else 4; 16 rows become 8), 2..6 = TMA-staged with that many planes where
+                                  the rows have that shape, -1 = register kernel */
 } ptk_server_config;
 
 typedef struct ptk_request_info {
@@ -275,6 +278,11 @@ typedef struct ptk_server_stats {
     long long chunks, kernel_launches;
     int peak_active;
     size_t peak_bytes;
+    /* where wall_s went: device time of the replayed chunks (CUDA events around each replay), and
+     * host time spent admitting requests (allocation, problem generation, material index, tensor
+     * maps), retiring them (checksums, result copies) and scheduling (work list, graph capture) */
+    double chunk_device_s, admit_s, retire_s, schedule_s;
+    long long graph_captures;
 } ptk_server_stats;
 
 int ptk_server_create(const ptk_server_config *cfg, ptk_server **out);

@@ -73,14 +73,45 @@ __global__ void k_generate_table(BoxArgs boxes, float dt, float eps0, float mu0,
 }
 
 // Sum of each valid field element (FP64; order of accumulation not fixed, for reporting only).
-__global__ void k_checksum(const float *__restrict__ f, int ex, int ey, int ez, int pitch, long long plane,
-                           double *out)
+// FP64 sums of an instance's six result fields in two launches with a fixed summation order (the
+// same request gives the same checksum bits every time): blocks sum strided rows into partials,
+// then one warp per field adds the partials.
+constexpr int kSumBlocks = 96;   // partial sums per field
+struct SumArgs {
+    const float *f[6];
+    int ex[6], ey[6], ez[6];
+    int pitch;
+    long long plane;
+};
+
+__global__ void __launch_bounds__(256) k_checksum_partial(SumArgs a, double *__restrict__ part)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y, k = blockIdx.z;
-    double v = (i < ex) ? (double)f[i + (long long)pitch * j + plane * k] : 0.0;
+    __shared__ double warp_sum[8];
+    const int f = blockIdx.y;
+    const int ex = a.ex[f], ey = a.ey[f], rows = a.ey[f] * a.ez[f];
+    const float *__restrict__ p = a.f[f];
+    double v = 0.0;
+    for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+        const float *__restrict__ row = p + (long long)a.pitch * (r % ey) + a.plane * (r / ey);
+        for (int i = threadIdx.x; i < ex; i += blockDim.x) v += (double)row[i];
+    }
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(out, v);
+    if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+        for (int w = 0; w < 8; ++w) b += warp_sum[w];
+        part[f * gridDim.x + blockIdx.x] = b;
+    }
+}
+
+__global__ void k_checksum_final(const double *__restrict__ part, int nb, double *__restrict__ out)
+{
+    const int f = threadIdx.y, lane = threadIdx.x;
+    double v = 0.0;
+    for (int b = lane; b < nb; b += 32) v += part[f * nb + b];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) out[f] = v;
 }
 
 struct Inst {
@@ -142,10 +173,15 @@ struct ptk_server {
     int depth_cap = 0;              // staged kernel: deepest z chunk of the current work list
     int resident = 1;               // CTAs of the step kernel that fit on the GPU at once
     int *h_err = nullptr;           // pinned copy, read after every chunk
+    double *d_part = nullptr;       // checksum partials (6 x kSumBlocks)
+    double *h_sums = nullptr;       // pinned landing slots of the checksums retired in a chunk
+    int sums_cap = 0;
     bool dirty = true;
     std::map<std::tuple<int, int, int, int, long long>, cudaGraphExec_t> graphs;
-    long long chunks = 0, launches = 0;
+    long long chunks = 0, launches = 0, captures = 0;
     double wall_s = 0, cell_updates = 0;
+    double chunk_dev_s = 0, admit_s = 0, retire_s = 0, sched_s = 0;   // where wall_s went
+    cudaEvent_t ev[2] = {nullptr, nullptr};                           // around each chunk replay
     double t0_wall = 0;
     std::mutex mu;
 };
@@ -210,7 +246,7 @@ int choose_depth_cap(const ptk_server *s)
         for (const Inst *in : s->active) {
             const int d = depth_for_cap(in->L.nz, cap);
             const int kc = d ? d : in->L.nz;
-            tiles += (long long)((in->L.nx + kTileX - 1) / kTileX) * ((in->L.ny + s->rows - 1) / s->rows) *
+            tiles += (long long)((in->L.nx + 32 * s->vec - 1) / (32 * s->vec)) * ((in->L.ny + s->rows - 1) / s->rows) *
                      ((in->L.nz + kc - 1) / kc);
         }
         if (tiles >= want) return cap;
@@ -334,9 +370,10 @@ int rebuild_worklist(ptk_server *s)
     int rc = grow_worklist(s, n);
     if (rc) return rc;
     cudaStreamSynchronize(s->st);   // the pinned staging may still feed a previous copy
-    // 128-wide tiles (4 cells per thread): narrower tiles keep more lanes busy on small grids but
-    // hold fewer bytes in flight per thread, and measured slower on the batched workload.
-    s->vec = 4;
+    // Register kernel: 128-wide tiles (4 cells per thread); narrower ones keep more lanes busy on
+    // small grids but hold fewer bytes in flight per thread, and measured slower on the batched
+    // workload.  The staged kernel's width goes with its rows (set at creation).
+    if (!s->stages) s->vec = 4;
     if (s->stages) {
         s->depth_cap = choose_depth_cap(s);
         // longest tiles first, so that the dynamic tile queue ends with short ones
@@ -407,39 +444,59 @@ int chunk_graph(ptk_server *s, int len, int grid, cudaGraphExec_t *out)
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return set_error(PTK_ERR_CUDA, "chunk instantiate: %s", cudaGetErrorString(e));
     s->graphs[key] = ex;
+    ++s->captures;
     *out = ex;
     return PTK_OK;
 }
 
-int retire(ptk_server *s, Inst *in, double t)
+// A finished instance's checksums (and, with keep_results, its result fields) are enqueued, and
+// its arrays freed (also on failure), in stream order; the checksums land in the pinned slot
+// h_slot, valid after the next synchronisation of the server's stream (retire_finish).
+int retire_copies(ptk_server *s, Inst *in, double *h_slot)
 {
     const int par = in->done & 1;
-    PTK_CUDA_TRY(cudaMemsetAsync(in->d_sum, 0, 6 * sizeof(double), s->st));
+    SumArgs a{};
     for (int f = 0; f < 6; ++f) {
-        int ex, ey, ez;
-        field_extents(f, in->L.nx, in->L.ny, in->L.nz, &ex, &ey, &ez);
-        dim3 grid((ex + 127) / 128, ey, ez);
-        k_checksum<<<grid, 128, 0, s->st>>>(in->buf[par][f], ex, ey, ez, in->L.pitch, in->L.plane, in->d_sum + f);
-        count_launches(1);
-        if (s->cfg.keep_results) {
-            in->result[f].resize((size_t)ex * ey * ez);
+        a.f[f] = in->buf[par][f];
+        field_extents(f, in->L.nx, in->L.ny, in->L.nz, &a.ex[f], &a.ey[f], &a.ez[f]);
+    }
+    a.pitch = in->L.pitch;
+    a.plane = in->L.plane;
+    k_checksum_partial<<<dim3(kSumBlocks, 6), 256, 0, s->st>>>(a, s->d_part);
+    k_checksum_final<<<1, dim3(32, 6), 0, s->st>>>(s->d_part, kSumBlocks, in->d_sum);
+    PTK_CUDA_TRY(cudaGetLastError());
+    count_launches(2);
+    PTK_CUDA_TRY(cudaMemcpyAsync(h_slot, in->d_sum, 6 * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+    if (s->cfg.keep_results) {
+        for (int f = 0; f < 6; ++f) {
+            in->result[f].resize((size_t)a.ex[f] * a.ey[f] * a.ez[f]);
             float *stage = nullptr;
             int rc = pool_alloc(in->result[f].size() * sizeof(float), s->st, (void **)&stage);
             if (rc) return rc;
-            rc = launch_unpack_field(in->buf[par][f], ex, ey, ez, in->L, stage, s->st);
+            rc = launch_unpack_field(in->buf[par][f], a.ex[f], a.ey[f], a.ez[f], in->L, stage, s->st);
             if (rc) return rc;
             PTK_CUDA_TRY(cudaMemcpyAsync(in->result[f].data(), stage, in->result[f].size() * sizeof(float),
                                          cudaMemcpyDeviceToHost, s->st));
             pool_free(stage, s->st);
         }
     }
-    PTK_CUDA_TRY(cudaMemcpyAsync(in->checksum, in->d_sum, 6 * sizeof(double), cudaMemcpyDeviceToHost, s->st));
-    PTK_CUDA_TRY(cudaStreamSynchronize(s->st));
+    return PTK_OK;
+}
+
+int retire_enqueue(ptk_server *s, Inst *in, double *h_slot)
+{
+    const int rc = retire_copies(s, in, h_slot);
+    release(s, in);
+    return rc;
+}
+
+// After the stream has been synchronised: the instance's checksums are in h_slot.
+void retire_finish(ptk_server *s, Inst *in, const double *h_slot, double t)
+{
+    for (int f = 0; f < 6; ++f) in->checksum[f] = h_slot[f];
     in->t_finish = t;
     in->finished = true;
     s->cell_updates += (double)in->L.nx * in->L.ny * in->L.nz * in->steps_total;
-    release(s, in);
-    return PTK_OK;
 }
 
 }  // namespace
@@ -458,7 +515,8 @@ int ptk_server_create(const ptk_server_config *cfg, ptk_server **out)
     if (s->cfg.chunk_steps <= 0) s->cfg.chunk_steps = 32;
     // default rows: 11 for the staged kernel (twelve warps per CTA; measured best), 8 otherwise
     if (s->cfg.tile_rows == 0) s->cfg.tile_rows = s->cfg.stages >= 0 ? 11 : 8;
-    const bool staged_rows = s->cfg.stages >= 0 && (s->cfg.tile_rows == 10 || s->cfg.tile_rows == 11);
+    const bool staged_rows = s->cfg.stages >= 0 && (s->cfg.tile_rows == 7 || s->cfg.tile_rows == 10 ||
+                                                    s->cfg.tile_rows == 11 || s->cfg.tile_rows == 23);
     if (s->cfg.tile_rows != 4 && s->cfg.tile_rows != 8 && s->cfg.tile_rows != 16 && !staged_rows) s->cfg.tile_rows = 8;
     s->rows = s->cfg.tile_rows;
     if (s->cfg.stages < 0) {
@@ -466,13 +524,19 @@ int ptk_server_create(const ptk_server_config *cfg, ptk_server **out)
     } else if (s->cfg.stages == 0) {
         if (s->rows == 16) s->rows = 8;
         s->stages = s->rows == 4 ? 3 : 4;
+        s->vec = yee_bulk_tile_vec(s->rows);
     } else {
         s->stages = s->cfg.stages;
+        s->vec = yee_bulk_tile_vec(s->rows);
         if (yee_bulk_smem_bytes(s->rows, s->stages, true) == 0) {
             delete s;
             return set_error(PTK_ERR_INVALID, "no staged kernel for %d rows with %d stages", cfg->tile_rows,
                              cfg->stages);
         }
+    }
+    if (pool_alloc(sizeof(double) * 6 * kSumBlocks, default_stream(), (void **)&s->d_part)) {
+        delete s;
+        return set_error(PTK_ERR_NOMEM, "server checksum partials allocation failed");
     }
     if (s->stages && (pool_alloc(sizeof(int), default_stream(), (void **)&s->d_err) ||
                       pool_alloc(sizeof(int) * s->cfg.chunk_steps, default_stream(), (void **)&s->d_work) ||
@@ -482,6 +546,7 @@ int ptk_server_create(const ptk_server_config *cfg, ptk_server **out)
         if (s->d_err) pool_free(s->d_err, default_stream());
         if (s->d_work) pool_free(s->d_work, default_stream());
         if (s->h_err) cudaFreeHost(s->h_err);
+        pool_free(s->d_part, default_stream());
         delete s;
         return set_error(PTK_ERR_CUDA, "server error word allocation failed");
     }
@@ -490,7 +555,11 @@ int ptk_server_create(const ptk_server_config *cfg, ptk_server **out)
         cudaMemGetInfo(&f, &t);
         s->cfg.hbm_budget_bytes = f / 10 * 8;
     }
-    if (cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&s->ev[0]) != cudaSuccess || cudaEventCreate(&s->ev[1]) != cudaSuccess) {
+        for (cudaEvent_t e : s->ev)
+            if (e) cudaEventDestroy(e);
+        if (s->st) cudaStreamDestroy(s->st);
         delete s;
         return set_error(PTK_ERR_CUDA, "stream creation failed");
     }
@@ -548,7 +617,9 @@ int ptk_server_run(ptk_server *s, double time_scale)
             const size_t need = instance_bytes(make_layout(in->desc.Nx, in->desc.Ny, in->desc.Nz), in->desc.steps);
             if (s->used + need > s->cfg.hbm_budget_bytes) break;
             in->t_admit = t;
+            const double ta = now_s();
             rc = admit(s, in);
+            s->admit_s += now_s() - ta;
             if (rc) break;
             ++nxt;
         }
@@ -560,6 +631,7 @@ int ptk_server_run(ptk_server *s, double time_scale)
             }
             continue;
         }
+        const double ts = now_s();
         if (s->dirty) rc = rebuild_worklist(s);
         if (rc) break;
         int left_min = 1 << 30;
@@ -570,12 +642,16 @@ int ptk_server_run(ptk_server *s, double time_scale)
         cudaGraphExec_t ex;
         rc = chunk_graph(s, len, grid, &ex);
         if (rc) break;
-        if (cudaGraphLaunch(ex, s->st) != cudaSuccess) {
+        s->sched_s += now_s() - ts;
+        if (cudaEventRecord(s->ev[0], s->st) != cudaSuccess || cudaGraphLaunch(ex, s->st) != cudaSuccess ||
+            cudaEventRecord(s->ev[1], s->st) != cudaSuccess) {
             rc = set_error(PTK_ERR_CUDA, "chunk launch failed");
             break;
         }
-        count_graph_launch(len + 1);
-        s->launches += len + 1;
+        // kernels in the chunk graph: the steps, the step-counter advance and (staged) the faces
+        const int kernels = len + 1 + (s->stages && s->total_faces > 0 ? 1 : 0);
+        count_graph_launch(kernels);
+        s->launches += kernels;
         ++s->chunks;
         if (s->stages && cudaMemcpyAsync(s->h_err, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->st) != cudaSuccess) {
             rc = set_error(PTK_ERR_CUDA, "error word copy failed");
@@ -589,19 +665,42 @@ int ptk_server_run(ptk_server *s, double time_scale)
             rc = set_error(PTK_ERR_TIMEOUT, "staged step kernel: a bounded wait expired (error word %d)", *s->h_err);
             break;
         }
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, s->ev[0], s->ev[1]) == cudaSuccess) s->chunk_dev_s += ms * 1e-3;
         t = clock();
-        std::vector<Inst *> still;
+        const double tr = now_s();
+        std::vector<Inst *> still, gone;
         for (Inst *in : s->active) {
             in->done += std::min(len, in->steps_total - in->done);
-            if (in->done >= in->steps_total) {
-                rc = retire(s, in, t);
-                if (rc) break;
-                s->dirty = true;
-            } else {
-                still.push_back(in);
-            }
+            (in->done >= in->steps_total ? gone : still).push_back(in);
         }
         s->active.swap(still);
+        if (!gone.empty()) {
+            // every finisher's checksums and frees in stream order, then one synchronisation
+            if ((int)gone.size() > s->sums_cap) {
+                if (s->h_sums) cudaFreeHost(s->h_sums);
+                s->h_sums = nullptr;
+                s->sums_cap = 0;
+                if (cudaMallocHost(&s->h_sums, sizeof(double) * 6 * gone.size()) != cudaSuccess) {
+                    for (Inst *in : gone) release(s, in);
+                    rc = set_error(PTK_ERR_NOMEM, "pinned checksum slots");
+                    break;
+                }
+                s->sums_cap = (int)gone.size();
+            }
+            for (size_t q = 0; q < gone.size(); ++q) {
+                if (!rc) rc = retire_enqueue(s, gone[q], s->h_sums + 6 * q);
+                else release(s, gone[q]);
+            }
+            if (rc) break;
+            if (cudaStreamSynchronize(s->st) != cudaSuccess) {
+                rc = set_error(PTK_ERR_CUDA, "retirement failed: %s", cudaGetErrorString(cudaGetLastError()));
+                break;
+            }
+            for (size_t q = 0; q < gone.size(); ++q) retire_finish(s, gone[q], s->h_sums + 6 * q, t);
+            s->dirty = true;
+        }
+        s->retire_s += now_s() - tr;
     }
     s->wall_s += clock();
     return rc;
@@ -664,6 +763,11 @@ int ptk_server_stats_get(ptk_server *s, ptk_server_stats *st)
     st->kernel_launches = s->launches;
     st->peak_active = s->peak_active;
     st->peak_bytes = s->peak_bytes;
+    st->chunk_device_s = s->chunk_dev_s;
+    st->admit_s = s->admit_s;
+    st->retire_s = s->retire_s;
+    st->schedule_s = s->sched_s;
+    st->graph_captures = s->captures;
     return PTK_OK;
 }
 
@@ -682,8 +786,12 @@ int ptk_server_destroy(ptk_server *s)
     if (s->d_err) pool_free(s->d_err, s->st);
     if (s->d_work) pool_free(s->d_work, s->st);
     if (s->h_err) cudaFreeHost(s->h_err);
+    if (s->d_part) pool_free(s->d_part, s->st);
+    if (s->h_sums) cudaFreeHost(s->h_sums);
     cudaStreamSynchronize(s->st);
     cudaStreamDestroy(s->st);
+    for (cudaEvent_t e : s->ev)
+        if (e) cudaEventDestroy(e);
     for (Inst *in : s->all) delete in;
     delete s;
     return PTK_OK;

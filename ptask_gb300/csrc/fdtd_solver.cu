@@ -153,10 +153,11 @@ static InstDesc host_desc(const ptk_solver *s, int steps_left)
         d.mat_tab = s->mat_tab;
         d.nmat = s->nmat;
     }
-    plan_tiles(d, rs.by, s->kc, s->vec);
+    plan_tiles(d, rs.by, s->kc, rs.stages > 0 ? yee_bulk_tile_vec(rs.by) : s->vec);
     if (rs.stages > 0) d.face_tiles = 0;   // faces: launch_yee_faces_steps, once per chunk
     return d;
 }
+
 
 static int solver_sync_desc(ptk_solver *s, int steps_left, cudaStream_t st)
 {
@@ -519,10 +520,10 @@ int ptk_solver_set_tiles(ptk_solver *s, const ptk_tile_config *cfg)
         if (vec == 0) vec = dv;
     }
     const int stages = cfg->stages;
-    if (stages > 0) vec = 4;
+    if (stages > 0) vec = yee_bulk_tile_vec(by);
     if (vec == 0) vec = default_vec(s->p.Nx);
-    PTK_CHECK_ARG(by == 4 || by == 8 || by == 16 || (stages > 0 && (by == 10 || by == 11)),
-                  "tile rows must be 4, 8 or 16, or 10 or 11 with a staged ring (got %d)", by);
+    PTK_CHECK_ARG(by == 4 || by == 8 || by == 16 || (stages > 0 && (by == 7 || by == 10 || by == 11 || by == 23)),
+                  "tile rows must be 4, 8 or 16, or 7, 10, 11 or 23 with a staged ring (got %d)", by);
     PTK_CHECK_ARG(vec == 1 || vec == 2 || vec == 4, "cells per thread must be 1, 2 or 4 (got %d)", vec);
     PTK_CHECK_ARG(stages == 0 || yee_bulk_smem_bytes(by, stages, false) > 0 || yee_bulk_smem_bytes(by, stages, true) > 0,
                   "no staged kernel for %d rows with %d stages", by, stages);
@@ -710,28 +711,53 @@ int ptk_autotune_tiles(int Nx, int Ny, int Nz, ptk_tile_config *best, float *bes
             add(by, vec, 0, yee_resident_ctas(by, vec));
         }
     // Staged shapes: timed on vacuum coefficients, i.e. with the material index where the shape has it.
-    const int staged[13][2] = {{4, 2}, {4, 3}, {4, 4}, {4, 5}, {4, 6}, {8, 2}, {8, 3}, {8, 4}, {8, 5}, {8, 6},
-                               {10, 4}, {10, 5}, {11, 4}};
+    const int staged[17][2] = {{4, 2}, {4, 3}, {4, 4}, {4, 5}, {4, 6}, {8, 2}, {8, 3}, {8, 4}, {8, 5}, {8, 6},
+                               {10, 4}, {10, 5}, {11, 4}, {23, 3}, {23, 4}, {7, 3}, {7, 4}};
     for (const auto &bs : staged) {
         const bool m = yee_bulk_smem_bytes(bs[0], bs[1], true) > 0;
-        add(bs[0], 4, bs[1], yee_bulk_resident_ctas(bs[0], bs[1], m));
+        add(bs[0], yee_bulk_tile_vec(bs[0]), bs[1], yee_bulk_resident_ctas(bs[0], bs[1], m));
     }
+    // ms per step of one shape over n steps after a 2-step warm-up (< 0: the shape does not run)
+    auto time_shape = [&](const ptk_tile_config &c, int n) -> float {
+        if (ptk_solver_set_tiles(s, &c)) return -1.f;
+        if (ptk_solver_run(s, 2, st)) return -2.f;
+        cudaEventRecord(e0, st);
+        if (ptk_solver_run(s, n, st)) return -2.f;
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        return ms / n;
+    };
+    // First pass: every candidate, briefly.  Second pass: the closest few again over longer runs,
+    // twice in alternating order, since shapes within a few per cent of each other trade places
+    // in short timings.
+    std::vector<std::pair<float, ptk_tile_config>> timed;
     for (const ptk_tile_config &c : cands) {
-        {
-            if (ptk_solver_set_tiles(s, &c)) continue;
-            if (ptk_solver_run(s, 2, st)) { rc = PTK_ERR_CUDA; break; }
-            cudaEventRecord(e0, st);
-            if (ptk_solver_run(s, steps, st)) { rc = PTK_ERR_CUDA; break; }
-            cudaEventRecord(e1, st);
-            cudaEventSynchronize(e1);
-            float ms = 0;
-            cudaEventElapsedTime(&ms, e0, e1);
-            ms /= steps;
-            if (ms < best_t) {
-                best_t = ms;
-                bc = c;
+        const float ms = time_shape(c, steps);
+        if (ms == -2.f) { rc = PTK_ERR_CUDA; break; }
+        if (ms > 0) timed.push_back({ms, c});
+    }
+    if (!rc && !timed.empty()) {
+        std::stable_sort(timed.begin(), timed.end(),
+                         [](const std::pair<float, ptk_tile_config> &a, const std::pair<float, ptk_tile_config> &b) {
+                             return a.first < b.first;
+                         });
+        std::vector<std::pair<float, ptk_tile_config>> top;
+        for (const auto &e : timed)
+            if (top.size() < 4 && e.first <= timed[0].first * 1.05f) top.push_back({0.f, e.second});
+        for (int pass = 0; pass < 2 && !rc && top.size() > 1; ++pass)
+            for (size_t q = 0; q < top.size() && !rc; ++q) {
+                auto &e = top[pass ? top.size() - 1 - q : q];
+                const float ms = time_shape(e.second, 3 * steps);
+                if (ms < 0) rc = PTK_ERR_CUDA; else e.first += ms;
             }
-        }
+        if (top.size() == 1) top[0].first = 2 * timed[0].first;
+        for (const auto &e : top)
+            if (e.first / 2 < best_t) {
+                best_t = e.first / 2;
+                bc = e.second;
+            }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

@@ -35,8 +35,23 @@ namespace ptk {
 
 namespace {
 
-constexpr int kRowW = 136;      // staged float row: x0-4 .. x0+131 (16-byte aligned ends)
-constexpr int kRowB8 = 160;     // staged material-index row (bytes): x0-16 .. x0+143
+// Tile width W (cells): 128 (a warp per row, 4 cells per lane) or 64 (a warp per two rows, 16
+// lanes per row).  A staged float row covers x0-4 .. x0+W+3 and a material-index row x0-16 ..
+// x0+W+15, so that both start and end on 16-byte boundaries.
+template <int W>
+__host__ __device__ constexpr int row_w() { return W + 8; }
+template <int W>
+__host__ __device__ constexpr int row_b8() { return W + 32; }
+template <int W>
+__host__ __device__ constexpr int lanes_per_row() { return W / 4; }
+template <int W>
+__host__ __device__ constexpr int rows_per_warp() { return 32 / lanes_per_row<W>(); }
+// Rows that go with a tile width: 7- and 23-row tiles are 64 cells wide (four and twelve warps),
+// all others 128.
+__host__ __device__ constexpr int width_of(int by) { return (by == 7 || by == 23) ? 64 : 128; }
+// CTAs per SM the instantiation is compiled for: four-warp CTAs (7 rows) run three to an SM, each
+// with its own plane barrier; the others one.
+__host__ __device__ constexpr int ctas_per_sm(int by) { return by == 7 ? 3 : 1; }
 constexpr int kWaitLimit = 1 << 22;
 constexpr int kMapMat = 16;     // tensor map of the material index in an instance's set
 constexpr size_t kTabBytes = 256 * sizeof(float4);   // material table (Ca, Cb, Da, Db) per entry
@@ -57,11 +72,11 @@ template <int BY>
 __host__ __device__ constexpr int row_hi(int a) { return (a == A_EX || a == A_EZ) ? BY + 2 : BY + 1; }
 template <int BY, bool MAT>
 __host__ __device__ constexpr int rows_of(int a) { return row_hi<BY>(a) - row_lo<MAT>(a); }
-template <bool MAT>
-__host__ __device__ constexpr int row_bytes(int a) { return is_u8<MAT>(a) ? kRowB8 : kRowW * 4; }
+template <bool MAT, int W = 128>
+__host__ __device__ constexpr int row_bytes(int a) { return is_u8<MAT>(a) ? row_b8<W>() : row_w<W>() * 4; }
 // Each array's region in a stage starts on a 128-byte boundary (TMA destination alignment).
-template <int BY, bool MAT>
-__host__ __device__ constexpr int region_bytes(int a) { return (rows_of<BY, MAT>(a) * row_bytes<MAT>(a) + 127) / 128 * 128; }
+template <int BY, bool MAT, int W = width_of(BY)>
+__host__ __device__ constexpr int region_bytes(int a) { return (rows_of<BY, MAT>(a) * row_bytes<MAT, W>(a) + 127) / 128 * 128; }
 template <int BY, bool MAT>
 __host__ __device__ constexpr int region_off(int a)
 {
@@ -72,7 +87,7 @@ __host__ __device__ constexpr int region_off(int a)
 template <int BY, bool MAT>
 __host__ __device__ constexpr size_t stage_bytes() { return (size_t)region_off<BY, MAT>(n_arrays<MAT>()); }
 template <int BY, bool MAT>
-__host__ __device__ constexpr uint32_t box_bytes(int a) { return (uint32_t)(rows_of<BY, MAT>(a) * row_bytes<MAT>(a)); }
+__host__ __device__ constexpr uint32_t box_bytes(int a) { return (uint32_t)(rows_of<BY, MAT>(a) * row_bytes<MAT, width_of(BY)>(a)); }
 template <int BY, bool MAT>
 __host__ __device__ constexpr uint32_t plane_tx_bytes()
 {
@@ -80,8 +95,11 @@ __host__ __device__ constexpr uint32_t plane_tx_bytes()
     for (int a = 0; a < n_arrays<MAT>(); ++a) t += box_bytes<BY, MAT>(a);
     return t;
 }
+// Threads of a CTA: one per 4 cells of the tile's BY rows and its y-1 halo row.
 template <int BY>
-__host__ __device__ constexpr size_t xchg_bytes() { return (size_t)2 * 2 * (BY + 1) * 32 * sizeof(float4); }
+__host__ __device__ constexpr int warps_of() { return (BY + 1) / rows_per_warp<width_of(BY)>(); }
+template <int BY>
+__host__ __device__ constexpr size_t xchg_bytes() { return (size_t)2 * 2 * (BY + 1) * lanes_per_row<width_of(BY)>() * sizeof(float4); }
 // [S stages][H exchange][material table (MAT)][S mbarriers][tile slot]
 template <int BY, int S, bool MAT>
 __host__ __device__ constexpr size_t smem_bytes()
@@ -167,14 +185,14 @@ __device__ __forceinline__ void issue_plane(const CUtensorMap *set, int par, int
 template <int BY, bool MAT>
 __device__ __forceinline__ const float *row_ptr(const unsigned char *st, int a, int r)
 {
-    return reinterpret_cast<const float *>(st + region_off<BY, MAT>(a)) + (size_t)(r - row_lo<MAT>(a)) * kRowW;
+    return reinterpret_cast<const float *>(st + region_off<BY, MAT>(a)) + (size_t)(r - row_lo<MAT>(a)) * row_w<width_of(BY)>();
 }
 
 // Material-index row of frame row r; byte 16 + c is the node at x0 + c.
 template <int BY>
 __device__ __forceinline__ const unsigned char *row_mat(const unsigned char *st, int r)
 {
-    return st + region_off<BY, true>(A_MT) + (size_t)r * kRowB8;
+    return st + region_off<BY, true>(A_MT) + (size_t)r * row_b8<width_of(BY)>();
 }
 
 }  // namespace
@@ -204,13 +222,13 @@ __device__ __forceinline__ bool tile_at(int t, const InstDesc *__restrict__ inst
     r0 /= D->tiles_x;
     const int yt = r0 % D->tiles_y;
     const int zt = r0 / D->tiles_y;
-    T.D = D;
-    T.maps = reinterpret_cast<const CUtensorMap *>(D->tma);
-    T.par = (D->step + s_off) & 1;
-    T.x0 = xt * 128;
+    T.x0 = xt * width_of(BY);
     T.y0 = yt * BY;
     T.k0 = zt * D->kc;
     T.k1 = min(T.k0 + D->kc, D->nz);
+    T.D = D;
+    T.maps = reinterpret_cast<const CUtensorMap *>(D->tma);
+    T.par = (D->step + s_off) & 1;
     T.kstart = T.k0 > 0 ? T.k0 - 1 : T.k0;
     T.nplanes = T.k1 - T.kstart + 1;
     return true;
@@ -221,14 +239,17 @@ __device__ __forceinline__ bool tile_at(int t, const InstDesc *__restrict__ inst
 // next tile while it works on the current one, and once the current tile's planes are all in
 // flight the refills continue with the next tile's, so a tile starts without a pipeline fill.
 template <int BY, int S, bool MAT>
-__global__ void __launch_bounds__(32 * (BY + 1), 1)
+__global__ void __launch_bounds__(32 * warps_of<BY>(), ctas_per_sm(BY))
 k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile0, int ninst, int s_off,
                 int total_tiles, int *err, int *work)
 {
     constexpr size_t SB = stage_bytes<BY, MAT>();
     extern __shared__ __align__(128) unsigned char smem[];
     unsigned char *stages = smem;
-    float4 *xchg = reinterpret_cast<float4 *>(smem + S * SB);   // [2 buf][2 arr][BY+1][32]
+    constexpr int LW = lanes_per_row<width_of(BY)>();   // lanes per tile row
+    constexpr int RPW = rows_per_warp<width_of(BY)>();   // tile rows per warp
+    static_assert((BY + 1) % RPW == 0, "a warp holds whole rows of the frame");
+    float4 *xchg = reinterpret_cast<float4 *>(smem + S * SB);   // [2 buf][2 arr][BY+1][LW]
     float4 *tab = reinterpret_cast<float4 *>(smem + S * SB + xchg_bytes<BY>());   // MAT: (Ca, Cb, Da, Db)[256]
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + S * SB + xchg_bytes<BY>() + (MAT ? kTabBytes : 0));
     int *slot = reinterpret_cast<int *>(bars + S);   // next tile, handed to the whole CTA
@@ -308,7 +329,7 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
             // The previous tile ended with a block barrier: nobody reads the old table any more.
             if (D->mat_tab != tab_src) {
                 const float4 *src_tab = reinterpret_cast<const float4 *>(D->mat_tab);
-                for (int m = ty * 32 + lane; m < D->nmat; m += 32 * (BY + 1)) tab[m] = __ldg(src_tab + m);
+                for (int m = ty * 32 + lane; m < D->nmat; m += 32 * warps_of<BY>()) tab[m] = __ldg(src_tab + m);
                 tab_src = D->mat_tab;
                 __syncthreads();
             }
@@ -329,15 +350,16 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
         const long long src = D->src;
         const float srcv = (src >= 0 && step < D->nwave) ? __ldg(D->wave + step) : 0.f;
 
-        const int i = x0 + 4 * lane;
-        const int r = ty;                 // frame row of this thread
-        const int j = y0 + ty - 1;
-        const bool halo = (ty == 0);
+        const int lx = lane % LW;         // this thread's 4 cells in its row
+        const int r = ty * RPW + lane / LW;   // frame row of this thread
+        const int i = x0 + 4 * lx;
+        const int j = y0 + r - 1;
+        const bool halo = (r == 0);
         const bool xin = (i <= nx);
         const bool jrow = (j >= 0 && j < ny);
         const int nout = min(4, nx - i);
-        const bool hcol = (!halo) && (lane == 0) && (x0 > 0) && jrow;
-        const int xl = 4 + 4 * lane;      // local x of this thread's first cell in a staged row
+        const bool hcol = (!halo) && (lx == 0) && (x0 > 0) && jrow;
+        const int xl = 4 + 4 * lx;        // local x of this thread's first cell in a staged row
         long long off = (long long)i + (long long)pitch * (j < 0 ? 0 : j) + plane * kstart;
 
         float4 hxp = make_float4(0, 0, 0, 0), hyp = make_float4(0, 0, 0, 0);
@@ -371,7 +393,7 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
                 hz = ld4s(row_ptr<BY, MAT>(cur, A_HZ, r) + xl);
                 if constexpr (MAT) {
                     // four material ids, one per cell, then their (Ca, Cb, Da, Db) from the table
-                    const uint32_t ids = *reinterpret_cast<const uint32_t *>(row_mat<BY>(cur, r) + 16 + 4 * lane);
+                    const uint32_t ids = *reinterpret_cast<const uint32_t *>(row_mat<BY>(cur, r) + 16 + 4 * lx);
                     const float4 m0 = tab[ids & 255u], m1 = tab[(ids >> 8) & 255u];
                     const float4 m2 = tab[(ids >> 16) & 255u], m3 = tab[ids >> 24];
                     ca = make_float4(m0.x, m1.x, m2.x, m3.x);
@@ -390,15 +412,15 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
                         cb = ld4s(row_ptr<BY, MAT>(cur, A_CB, r) + xl);
                     }
                 }
-                if (lane == 31) {
+                if (lx == LW - 1) {
                     ez_l = row_ptr<BY, MAT>(cur, A_EZ, r)[xl + 4];
                     ey_l = row_ptr<BY, MAT>(cur, A_EY, r)[xl + 4];
                 }
             }
-            // x+1 neighbours
-            float ez_n = __shfl_down_sync(0xffffffffu, ez.x, 1);
-            float ey_n = __shfl_down_sync(0xffffffffu, ey0.x, 1);
-            if (lane == 31) { ez_n = ez_l; ey_n = ey_l; }
+            // x+1 neighbours (shuffles within each row's LW lanes)
+            float ez_n = __shfl_down_sync(0xffffffffu, ez.x, 1, LW);
+            float ey_n = __shfl_down_sync(0xffffffffu, ey0.x, 1, LW);
+            if (lx == LW - 1) { ez_n = ez_l; ey_n = ey_l; }
             const float ezv[4] = {ez.x, ez.y, ez.z, ez.w}, eyv[4] = {ey0.x, ey0.y, ey0.z, ey0.w};
             const float ez_ip[4] = {ez.y, ez.z, ez.w, ez_n}, ey_ip[4] = {ey0.y, ey0.z, ey0.w, ey_n};
             const float hxv[4] = {hx.x, hx.y, hx.z, hx.w}, hyv[4] = {hy.x, hy.y, hy.z, hy.w};
@@ -432,23 +454,23 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
                 hyh = yee_b(dah, Hy[3], dbh, ez.x, Ez[3], cx, Exn[3], Ex[3], cz);
                 hzh = yee_b(dah, Hz[3], dbh, Exj[3], Ex[3], cy, ey0.x, Ey[3], cx);
             }
-            float4 *sH = xchg + (size_t)(q & 1) * 2 * (BY + 1) * 32;   // [arr][row][lane]
+            float4 *sH = xchg + (size_t)(q & 1) * 2 * (BY + 1) * LW;   // [arr][row][x lane]
             if (!warm) {
-                sH[ty * 32 + lane] = make_float4(hxn[0], hxn[1], hxn[2], hxn[3]);
-                sH[(BY + 1) * 32 + ty * 32 + lane] = make_float4(hzn[0], hzn[1], hzn[2], hzn[3]);
+                sH[r * LW + lx] = make_float4(hxn[0], hxn[1], hxn[2], hxn[3]);
+                sH[(BY + 1) * LW + r * LW + lx] = make_float4(hzn[0], hzn[1], hzn[2], hzn[3]);
             }
             __syncthreads();
             // Plane k's stage was read (as "next") before the previous barrier and (as "current")
             // before this one, and nothing after this barrier reads a stage: refill it now (with a
             // plane of the next tile once this tile's planes are all in flight).
             if (ty == 0) top_up(gbase + q + 1 + S);
-            float hy_p = __shfl_up_sync(0xffffffffu, hyn[3], 1);
-            float hz_p = __shfl_up_sync(0xffffffffu, hzn[3], 1);
-            if (lane == 0) { hy_p = hyh; hz_p = hzh; }
+            float hy_p = __shfl_up_sync(0xffffffffu, hyn[3], 1, LW);
+            float hz_p = __shfl_up_sync(0xffffffffu, hzn[3], 1, LW);
+            if (lx == 0) { hy_p = hyh; hz_p = hzh; }
             if (!halo && jrow && xin) {
                 if (!warm) {
-                    const float4 hxj4 = sH[(ty - 1) * 32 + lane];
-                    const float4 hzj4 = sH[(BY + 1) * 32 + (ty - 1) * 32 + lane];
+                    const float4 hxj4 = sH[(r - 1) * LW + lx];
+                    const float4 hzj4 = sH[(BY + 1) * LW + (r - 1) * LW + lx];
                     const float hxj[4] = {hxj4.x, hxj4.y, hxj4.z, hxj4.w}, hzj[4] = {hzj4.x, hzj4.y, hzj4.z, hzj4.w};
                     const float cav[4] = {ca.x, ca.y, ca.z, ca.w}, cbv[4] = {cb.x, cb.y, cb.z, cb.w};
                     const float hxpv[4] = {hxp.x, hxp.y, hxp.z, hxp.w}, hypv[4] = {hyp.x, hyp.y, hyp.z, hyp.w};
@@ -598,7 +620,7 @@ static int resident_bulk()
 {
     if (prepare_bulk<BY, S, MAT>()) return 0;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_yee_step_bulk<BY, S, MAT>, 32 * (BY + 1),
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_yee_step_bulk<BY, S, MAT>, 32 * warps_of<BY>(),
                                                       smem_bytes<BY, S, MAT>()) != cudaSuccess)
         return 0;
     return per_sm * std::max(1, sm_count());
@@ -612,7 +634,7 @@ static int launch_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, i
     int rc = prepare_bulk<BY, S, MAT>();
     if (rc) return rc;
     const int g = (grid <= 0 || grid > total_tiles) ? total_tiles : grid;
-    k_yee_step_bulk<BY, S, MAT><<<g, dim3(32, BY + 1), smem, s>>>(d_insts, d_tile0, ninst, s_offset, total_tiles,
+    k_yee_step_bulk<BY, S, MAT><<<g, dim3(32, warps_of<BY>()), smem, s>>>(d_insts, d_tile0, ninst, s_offset, total_tiles,
                                                                   err, work);
     PTK_CUDA_TRY(cudaGetLastError());
     count_launches(1);
@@ -626,7 +648,8 @@ static int launch_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, i
     X(8, 2, false) X(8, 3, false) X(8, 4, false) X(10, 3, false) X(11, 3, false)
 #define PTK_MAT_SHAPES(X) X(4, 2, true) X(4, 3, true) X(4, 4, true) X(4, 5, true) X(4, 6, true) \
     X(8, 2, true) X(8, 3, true) X(8, 4, true) X(8, 5, true) X(8, 6, true) \
-    X(10, 4, true) X(10, 5, true) X(11, 4, true)
+    X(10, 4, true) X(10, 5, true) X(11, 4, true) X(23, 3, true) X(23, 4, true) \
+    X(7, 3, true) X(7, 4, true)
 
 int launch_yee_step_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles, int s_offset,
                          int by, int stages, int grid, int *err, cudaStream_t s, int *work, bool mat)
@@ -640,6 +663,8 @@ int launch_yee_step_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst,
     return set_error(PTK_ERR_INVALID, "no staged kernel for %d rows x %d stages%s", by, stages,
                      mat ? " with a material index" : "");
 }
+
+int yee_bulk_tile_vec(int by) { return width_of(by) / 32; }
 
 size_t yee_bulk_smem_bytes(int by, int stages, bool mat)
 {
@@ -692,7 +717,8 @@ static int encode_set(const InstDesc &d, CUtensorMap *out)
         const bool u8 = m == kMapMat;
         const int a = m < 12 ? m % 6 : (u8 ? A_MT : 6 + (m - 12));
         void *base = m < 12 ? (void *)d.buf[m / 6][m % 6] : u8 ? (void *)d.mat : (void *)d.coef[m - 12];
-        const cuuint32_t box[3] = {(cuuint32_t)(u8 ? kRowB8 : kRowW), (cuuint32_t)(u8 ? rows_of<BY, true>(a) : rows_of<BY, false>(a)), 1};
+        const cuuint32_t box[3] = {(cuuint32_t)(u8 ? row_b8<width_of(BY)>() : row_w<width_of(BY)>()),
+                                   (cuuint32_t)(u8 ? rows_of<BY, true>(a) : rows_of<BY, false>(a)), 1};
         CUresult r = enc(&out[m], u8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims,
                          u8 ? strides8 : strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -708,6 +734,8 @@ int encode_tma_set(const InstDesc &d, int by, void *host_out)
     if (by == 8) return encode_set<8>(d, out);
     if (by == 10) return encode_set<10>(d, out);
     if (by == 11) return encode_set<11>(d, out);
+    if (by == 23) return encode_set<23>(d, out);
+    if (by == 7) return encode_set<7>(d, out);
     return set_error(PTK_ERR_INVALID, "no staged kernel for %d rows", by);
 }
 

@@ -128,6 +128,9 @@ int launch_yee_step_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst,
 int launch_yee_faces_steps(const InstDesc *d_insts, const long long *d_face0, int ninst, long long total_faces,
                            int s_offset, int len, cudaStream_t s);
 long long face_nodes(int nx, int ny, int nz);
+// Cells per thread of the tile width that goes with `by` staged rows (plan_tiles' vec): 23-row
+// tiles are 64 cells wide (2), all others 128 (4).
+int yee_bulk_tile_vec(int by);
 // Shared memory of a staged instantiation (0: no such kernel).
 size_t yee_bulk_smem_bytes(int by, int stages, bool mat = false);
 // CTAs of the staged kernel that fit on the whole GPU at once (0: no such kernel).

@@ -159,7 +159,8 @@ class Solver:
     def set_tiles(self, by: int, kc: int, vec: int = 0, stages: int = 0) -> None:
         """Fused-kernel tile shape: `by` rows, `kc` z-planes (0 = all), `vec` x cells per thread
         (1, 2, 4; 0 = chosen from Nx), `stages` > 0 selects the kernel whose operands are staged in
-        shared memory by TMA tensor copies (that many planes in the ring, 2..5)."""
+        shared memory by TMA tensor copies (that many planes in the ring, 2..6; 7 and 23 rows give
+        64-wide tiles)."""
         call("ptk_solver_set_tiles", self._h, C.byref(TileConfig(by, kc, vec, stages)))
 
     def use_material_index(self, enable: bool = True, stream=None) -> None:
@@ -233,9 +234,9 @@ __all__ = ["FIELDS", "Problem", "Solver", "solve", "field_extents", "field_shape
            "random_fields", "reference_params", "launch_count", "device_info", "PTK_HOST", "PTK_DEVICE"]
 
 
-def tuned_tiles(nx: int, ny: int, nz: int) -> tuple[int, int, int]:
-    """Fastest (rows, z depth, x cells per thread) of the fused step kernel for this grid
-    (autotuned on the device, cached per process)."""
+def tuned_tiles(nx: int, ny: int, nz: int) -> tuple[int, int, int, int]:
+    """Fastest (rows, z depth, x cells per thread, staged planes) of the fused step kernel for this
+    grid (autotuned on the device, cached per process)."""
     t = TileConfig()
     ms = C.c_float()
     call("ptk_autotune_tiles", nx, ny, nz, C.byref(t), C.byref(ms))

@@ -314,9 +314,9 @@ def test_staged_kernel_small_and_edge_shapes(shape):
     p = P.reference_params(*shape)
     f = P.random_fields(*shape, seed=72)
     ref = oracle.step_ref_f32(f, steps, p)
-    for by, stages in ((8, 2), (4, 5)):
+    for by, stages, kc in ((8, 2, 3), (4, 5, 3), (23, 4, 3), (7, 4, 3), (11, 4, 0)):   # 7, 23 rows: 64 wide
         with P.Solver(p) as s:
-            s.set_tiles(by, 3, 4, stages)
+            s.set_tiles(by, kc, 4, stages)
             s.set_fields(f)
             s.set_vacuum()
             s.run(steps)
@@ -326,7 +326,8 @@ def test_staged_kernel_small_and_edge_shapes(shape):
 # ------------------------------------------------------------------------------------------------
 # Material index: one byte per node + a table instead of the four coefficient arrays.
 # ------------------------------------------------------------------------------------------------
-@pytest.mark.parametrize("by,stages", [(8, 4), (8, 6), (4, 3), (4, 5), (8, 2), (10, 4), (10, 5), (11, 4)])
+@pytest.mark.parametrize("by,stages", [(8, 4), (8, 6), (4, 3), (4, 5), (8, 2), (10, 4), (10, 5), (11, 4), (23, 3),
+                                      (23, 4), (7, 3), (7, 4)])
 def test_material_index_equals_per_cell_arrays(by, stages):
     shape, steps = (261, 37, 23), 7
     pr = P.Problem.generate(*shape, n_boxes=5, eps=(1, 10), box=(5, 30), steps=steps, seed=15)
@@ -340,7 +341,7 @@ def test_material_index_equals_per_cell_arrays(by, stages):
             s.use_material_index(use)
             assert (s.material_count() > 0) == use and s.material_count() <= 6
             st, mat = s.kernel()
-            dense = {4: (2, 3, 4, 5), 8: (2, 3, 4), 10: (3,), 11: (3,)}   # per-cell-array instantiations
+            dense = {4: (2, 3, 4, 5), 8: (2, 3, 4), 10: (3,), 11: (3,), 23: (), 7: ()}   # per-cell-array kernels
             fallback = stages if stages in dense[by] else (3 if 3 in dense[by] else 4)
             assert mat == use and st == (stages if use else fallback)
             s.set_fields(f)
@@ -381,7 +382,7 @@ def test_staged_full_size_matches_register_kernel(full_problem):
     pr = full_problem
     f = P.zero_fields(*FULL)
     outs = []
-    for tiles in ((4, 8, 4, 0), (8, 32, 4, 3), (4, 0, 4, 4)):
+    for tiles in ((4, 8, 4, 0), (8, 32, 4, 3), (4, 0, 4, 4), (11, 86, 4, 4), (23, 86, 2, 4), (7, 86, 2, 4)):
         with P.Solver(pr.params) as s:
             s.set_tiles(*tiles)
             s.set_fields(f)

@@ -17,7 +17,7 @@ def alone(r: Request):
     return P.solve(pr, P.zero_fields(r.nx, r.ny, r.nz), r.steps), pr
 
 
-@pytest.mark.parametrize("rows,stages", [(0, 0), (8, 0), (8, -1), (4, 3), (8, 2), (10, 5)])
+@pytest.mark.parametrize("rows,stages", [(0, 0), (8, 0), (8, -1), (4, 3), (8, 2), (10, 5), (23, 0), (23, 3), (7, 4)])
 def test_mixed_batch_results_equal_alone(rows, stages):
     """Staged (default ring, 2-plane ring, 4 rows) and register kernels all give the solo results."""
     reqs = [Request(24, 20, 16, 40, 2, 1), Request(37, 29, 23, 75, 3, 2), Request(64, 48, 40, 33, 1, 3),
@@ -32,6 +32,22 @@ def test_mixed_batch_results_equal_alone(rows, stages):
             ref, _ = alone(r)
             for q in range(6):
                 np.testing.assert_array_equal(got[q], ref[q], err_msg=f"request {t} field {P.FIELDS[q]}")
+
+
+def test_checksums_are_fp64_sums_and_deterministic():
+    """A request's checksums are the FP64 sums of its six result fields, with the same bits on every run."""
+    reqs = [Request(24, 20, 16, 40, 2, 21), Request(130, 37, 29, 25, 3, 22), Request(9, 70, 33, 18, 1, 23)]
+    runs = []
+    for _ in range(2):
+        with Server(keep_results=True, chunk_steps=16) as s:
+            tickets = [s.submit(r) for r in reqs]
+            s.run(time_scale=0)
+            runs.append([(list(s.info(t).checksum), s.fetch(t)) for t in tickets])
+    for (sums_a, fields), (sums_b, _) in zip(*runs):
+        assert sums_a == sums_b
+        for q in range(6):
+            f64 = fields[q].astype(np.float64)
+            assert abs(sums_a[q] - f64.sum()) <= 1e-12 * max(np.abs(f64).sum(), 1e-300)
 
 
 def test_batched_small_requests_match_oracle():
