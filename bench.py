@@ -300,14 +300,19 @@ def run_ours(args, wl, world, rank, local):
     h2d = sum(a.nbytes for a in zero) + 4 * prob.Ca.nbytes + prob.wave.nbytes
     d2h = sum(a.nbytes for a in zero)
 
-    phase_ev = [Event() for _ in range(4)]
-    phase_ms = {"upload": 0.0, "solve": 0.0, "download": 0.0}
+    phase_ev = [Event() for _ in range(6)]
+    phase_ms = {"upload": 0.0, "solve": 0.0, "download": 0.0,
+                "upload_fields": 0.0, "upload_coefficients_and_index": 0.0}
 
     def e2e_step(record=False):
         if record:
             phase_ev[0].record()
         _lib.call("ptk_solver_set_fields", solver.handle, in_ptrs, _lib.PTK_HOST, None)
+        if record:
+            phase_ev[4].record()
         _lib.call("ptk_solver_set_coefficients", solver.handle, *[h.ptr.value for h in hcoef], _lib.PTK_HOST, None)
+        if record:
+            phase_ev[5].record()
         _lib.call("ptk_solver_set_source", solver.handle, *prob.src, hwave.ptr.value, prob.wave.size,
                   _lib.PTK_HOST, None)
         solver.reset_clock()
@@ -320,7 +325,8 @@ def run_ours(args, wl, world, rank, local):
         if record:
             phase_ev[3].record()
             phase_ev[3].sync()
-            for name, a, b in (("upload", 0, 1), ("solve", 1, 2), ("download", 2, 3)):
+            for name, a, b in (("upload", 0, 1), ("solve", 1, 2), ("download", 2, 3), ("upload_fields", 0, 4),
+                               ("upload_coefficients_and_index", 4, 5)):
                 phase_ms[name] += phase_ev[a].elapsed_ms(phase_ev[b])
 
     for _ in range(max(1, args.warmup)):
