@@ -107,13 +107,19 @@ __global__ void k_mat_insert(const float *Ca, const float *Cb, const float *Da, 
 {
     const float *c[4] = {Ca, Cb, Da, Db};
     const long long stride = (long long)gridDim.x * blockDim.x;
+    uint4 last = make_uint4(0, 0, 0, 0);   // the tuple this thread inserted last (already in the table)
+    bool have_last = false;
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < N.n; q += stride) {
         const uint4 key = tuple_at(c, N.offset(q));
         // lanes with the same tuple (all four words equal) let their lowest lane insert it
         const unsigned act = __activemask();
         const unsigned m = __match_any_sync(act, key.x) & __match_any_sync(act, key.y) &
                            __match_any_sync(act, key.z) & __match_any_sync(act, key.w);
-        if ((threadIdx.x & 31) == __ffs(m) - 1) insert(S, key);
+        if ((threadIdx.x & 31) == __ffs(m) - 1 && !(have_last && same(key, last))) {
+            insert(S, key);
+            last = key;
+            have_last = true;
+        }
     }
 }
 

@@ -749,7 +749,7 @@ int ptk_autotune_tiles(int Nx, int Ny, int Nz, ptk_tile_config *best, float *bes
         for (int pass = 0; pass < 2 && !rc && top.size() > 1; ++pass)
             for (size_t q = 0; q < top.size() && !rc; ++q) {
                 auto &e = top[pass ? top.size() - 1 - q : q];
-                const float ms = time_shape(e.second, 3 * steps);
+                const float ms = time_shape(e.second, std::max(8 * steps, 128));
                 if (ms < 0) rc = PTK_ERR_CUDA; else e.first += ms;
             }
         if (top.size() == 1) top[0].first = 2 * timed[0].first;

@@ -370,7 +370,9 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
             const unsigned char *cur = stages + (size_t)(Gc % S) * SB;
             const unsigned char *nxt = stages + (size_t)(Gn % S) * SB;
             if (!failed) {
-                bool ok = mbar_wait(&bars[Gc % S], (Gc / S) & 1);
+                // Within a tile, plane q's stage was waited for as "next" in iteration q-1, and it is
+                // refilled only after this iteration's barrier.
+                bool ok = q > 0 || mbar_wait(&bars[Gc % S], (Gc / S) & 1);
                 ok = ok && mbar_wait(&bars[Gn % S], (Gn / S) & 1);
                 if (!ok) {
                     failed = true;
