@@ -404,11 +404,13 @@ def run_served(args, kind, world, rank, local):
                 "in [32,192], steps uniform in [100,2000], 1-8 dielectric boxes, seeded sources, FP32")
     else:
         n = args.requests
-        reqs = poisson_trace(n, rate=200.0, seed=5 + rank)
+        reqs = poisson_trace(n, rate=args.rate, seed=5 + rank)
         scale = 1.0
-        desc = (f"served FDTD: Poisson arrivals 200 req/s, {n} requests (the workload's 20k-request trace "
-                "shortened), cube edge log-uniform in [24,256], steps uniform in [50,1000], FP32, "
-                "admission by HBM budget")
+        trace = ("the workload's 20k-request trace" if n == 20000 else
+                 "the workload's 20k-request trace shortened")
+        desc = (f"served FDTD: Poisson arrivals {args.rate:g} req/s, {n} requests ({trace}"
+                f"{'' if args.rate == 200.0 else '; the workload offers 200 req/s, this rate is below saturation'}), "
+                "cube edge log-uniform in [24,256], steps uniform in [50,1000], FP32, admission by HBM budget")
     cells = sum(r.cell_updates for r in reqs)
 
     def serve(max_active):
@@ -471,6 +473,8 @@ def main() -> int:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batched", "served"], default="plain256")
     ap.add_argument("--requests", type=int, default=1000, help="served workload: requests in the trace")
+    ap.add_argument("--rate", type=float, default=200.0,
+                    help="served workload: Poisson arrival rate, requests/s (200: the workload's rate)")
     ap.add_argument("--server-rows", type=int, default=0,
                     help="batched / served: staged tile rows (0: the server's default; 23: 64-wide tiles)")
     ap.add_argument("--tiles", default=None, help="fixed tile shape ROWS,DEPTH (skips the autotuner)")
