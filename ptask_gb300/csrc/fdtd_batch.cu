@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstring>
 #include <map>
 #include <mutex>
 #include <thread>
@@ -156,13 +157,13 @@ struct ptk_server {
     size_t next = 0;                // next request to admit (arrival order)
     size_t used = 0, peak_bytes = 0;
     int peak_active = 0;
-    // device work list
+    // device work list; its pinned host staging is double-buffered by `par` (below)
     InstDesc *d_desc = nullptr;
     int *d_tile0 = nullptr;
-    InstDesc *h_desc = nullptr;     // pinned staging
-    int *h_tile0 = nullptr;
+    InstDesc *h_desc[2] = {};
+    int *h_tile0[2] = {};
     long long *d_face0 = nullptr;   // staged kernel: prefix sums of the instances' face nodes
-    long long *h_face0 = nullptr;
+    long long *h_face0[2] = {};
     long long total_faces = 0;
     int cap = 0;
     int total_tiles = 0;
@@ -172,16 +173,27 @@ struct ptk_server {
     int *d_work = nullptr;          // staged kernel's tile counters, one per step of a chunk
     int depth_cap = 0;              // staged kernel: deepest z chunk of the current work list
     int resident = 1;               // CTAs of the step kernel that fit on the GPU at once
-    int *h_err = nullptr;           // pinned copy, read after every chunk
     double *d_part = nullptr;       // checksum partials (6 x kSumBlocks)
-    double *h_sums = nullptr;       // pinned landing slots of the checksums retired in a chunk
-    int sums_cap = 0;
+    // Pipelining: a chunk is queued while the previous one runs.  Chunk slot b (= `par` when it was
+    // launched) owns the pinned error-word copy, the checksum landing slots of its finishers and its
+    // events; the host staging of parity b (work list, admission uploads) is reused two chunks later.
+    int par = 0;
+    int *h_err = nullptr;           // pinned, two slots
+    double *h_sums[2] = {};
+    int sums_cap[2] = {};
+    unsigned char *h_up[2] = {};    // pinned admission uploads (tensor maps, waveforms)
+    size_t up_used[2] = {};
+    struct Flight {
+        bool on = false;
+        std::vector<Inst *> gone;   // instances that finish with this chunk (retired behind it)
+    } flight[2];
     bool dirty = true;
     std::map<std::tuple<int, int, int, int, long long>, cudaGraphExec_t> graphs;
     long long chunks = 0, launches = 0, captures = 0;
     double wall_s = 0, cell_updates = 0;
     double chunk_dev_s = 0, admit_s = 0, retire_s = 0, sched_s = 0;   // where wall_s went
-    cudaEvent_t ev[2] = {nullptr, nullptr};                           // around each chunk replay
+    cudaEvent_t ev_start[2] = {}, ev_end[2] = {};   // around each chunk replay, per slot
+    cudaEvent_t ev_ret[2] = {};                      // after the slot's retirement copies
     double t0_wall = 0;
     std::mutex mu;
 };
@@ -198,21 +210,28 @@ int grow_worklist(ptk_server *s, int n)
     if (n <= s->cap) return PTK_OK;
     int cap = std::max(n, 2 * s->cap);
     if (s->d_desc) {
-        cudaStreamSynchronize(s->st);
+        cudaStreamSynchronize(s->st);   // queued chunks read the old lists and staging
         pool_free(s->d_desc, s->st);
         pool_free(s->d_tile0, s->st);
         pool_free(s->d_face0, s->st);
-        cudaFreeHost(s->h_desc);
-        cudaFreeHost(s->h_tile0);
-        cudaFreeHost(s->h_face0);
+        for (int b = 0; b < 2; ++b) {
+            cudaFreeHost(s->h_desc[b]);
+            cudaFreeHost(s->h_tile0[b]);
+            cudaFreeHost(s->h_face0[b]);
+            s->h_desc[b] = nullptr;
+            s->h_tile0[b] = nullptr;
+            s->h_face0[b] = nullptr;
+        }
     }
     int rc = pool_alloc(sizeof(InstDesc) * cap, s->st, (void **)&s->d_desc);
     if (!rc) rc = pool_alloc(sizeof(int) * (cap + 1), s->st, (void **)&s->d_tile0);
     if (!rc) rc = pool_alloc(sizeof(long long) * (cap + 1), s->st, (void **)&s->d_face0);
     if (rc) return rc;
-    PTK_CUDA_TRY(cudaMallocHost(&s->h_desc, sizeof(InstDesc) * cap));
-    PTK_CUDA_TRY(cudaMallocHost(&s->h_tile0, sizeof(int) * (cap + 1)));
-    PTK_CUDA_TRY(cudaMallocHost(&s->h_face0, sizeof(long long) * (cap + 1)));
+    for (int b = 0; b < 2; ++b) {
+        PTK_CUDA_TRY(cudaMallocHost(&s->h_desc[b], sizeof(InstDesc) * cap));
+        PTK_CUDA_TRY(cudaMallocHost(&s->h_tile0[b], sizeof(int) * (cap + 1)));
+        PTK_CUDA_TRY(cudaMallocHost(&s->h_face0[b], sizeof(long long) * (cap + 1)));
+    }
     s->cap = cap;
     for (auto &kv : s->graphs) cudaGraphExecDestroy(kv.second);
     s->graphs.clear();
@@ -279,6 +298,34 @@ InstDesc instance_desc(const ptk_server *s, const Inst *in)
     return d;
 }
 
+constexpr size_t kUpBytes = 4u << 20;   // each half of the pinned admission-upload arena
+
+// Host-to-device copy through the pinned upload arena of parity `par`, so that it is queued without
+// waiting for the chunks ahead of it.  A half is reused two chunks later, when the chunk that its
+// copies preceded has completed.  Uploads larger than a half are copied after the queue drains.
+int stage_upload(ptk_server *s, void *dst, const void *src, size_t bytes)
+{
+    const size_t need = (bytes + 63) & ~(size_t)63;
+    if (need > kUpBytes) {
+        PTK_CUDA_TRY(cudaStreamSynchronize(s->st));
+        PTK_CUDA_TRY(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+        return PTK_OK;
+    }
+    if (!s->h_up[0]) {
+        for (int b = 0; b < 2; ++b) PTK_CUDA_TRY(cudaMallocHost(&s->h_up[b], kUpBytes));
+    }
+    size_t &used = s->up_used[s->par];
+    if (used + need > kUpBytes) {   // full: let every queued copy from either half run
+        PTK_CUDA_TRY(cudaStreamSynchronize(s->st));
+        s->up_used[0] = s->up_used[1] = 0;
+    }
+    unsigned char *p = s->h_up[s->par] + used;
+    memcpy(p, src, bytes);
+    used += need;
+    PTK_CUDA_TRY(cudaMemcpyAsync(dst, p, bytes, cudaMemcpyHostToDevice, s->st));
+    return PTK_OK;
+}
+
 int admit(ptk_server *s, Inst *in)
 {
     std::vector<BoxSpec> boxes;
@@ -326,8 +373,8 @@ int admit(ptk_server *s, Inst *in)
         in->nmat = ba.n + 1;
     }
     if (in->nwave) {
-        // pageable source: the copy is staged before this returns, so `wave` may go out of scope
-        PTK_CUDA_TRY(cudaMemcpyAsync(in->wave, wave.data(), wave.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+        rc = stage_upload(s, in->wave, wave.data(), wave.size() * sizeof(float));
+        if (rc) return rc;
         in->src = (long long)si + (long long)in->L.pitch * sj + in->L.plane * sk;
     }
     if (s->stages) {
@@ -335,7 +382,8 @@ int admit(ptk_server *s, Inst *in)
         alignas(64) unsigned char maps[kTmaSetBytes];
         rc = encode_tma_set(instance_desc(s, in), s->rows, maps);
         if (rc) return rc;
-        PTK_CUDA_TRY(cudaMemcpyAsync(in->tma, maps, kTmaSetBytes, cudaMemcpyHostToDevice, st));
+        rc = stage_upload(s, in->tma, maps, kTmaSetBytes);
+        if (rc) return rc;
     }
     in->bytes = instance_bytes(in->L, in->nwave);
     s->used += in->bytes;
@@ -369,7 +417,11 @@ int rebuild_worklist(ptk_server *s)
     const int n = (int)s->active.size();
     int rc = grow_worklist(s, n);
     if (rc) return rc;
-    cudaStreamSynchronize(s->st);   // the pinned staging may still feed a previous copy
+    // Staging of parity `par`: its last copies fed the chunk before the previous one, which has
+    // completed (the run loop lands every chunk before launching the next-but-one).
+    InstDesc *h_desc = s->h_desc[s->par];
+    int *h_tile0 = s->h_tile0[s->par];
+    long long *h_face0 = s->h_face0[s->par];
     // Register kernel: 128-wide tiles (4 cells per thread); narrower ones keep more lanes busy on
     // small grids but hold fewer bytes in flight per thread, and measured slower on the batched
     // workload.  The staged kernel's width goes with its rows (set at creation).
@@ -386,20 +438,20 @@ int rebuild_worklist(ptk_server *s)
     long long faces = 0;
     for (int q = 0; q < n; ++q) {
         const InstDesc d = instance_desc(s, s->active[q]);
-        s->h_desc[q] = d;
-        s->h_face0[q] = faces;
+        h_desc[q] = d;
+        h_face0[q] = faces;
         faces += face_nodes(d.nx, d.ny, d.nz);
-        s->h_tile0[q] = tiles;
+        h_tile0[q] = tiles;
         tiles += d.tiles_x * d.tiles_y * d.tiles_z + d.face_tiles;
     }
-    s->h_tile0[n] = tiles;
+    h_tile0[n] = tiles;
     s->total_tiles = tiles;
-    s->h_face0[n] = faces;
+    h_face0[n] = faces;
     s->total_faces = s->stages ? faces : 0;
-    if (n) {
-        PTK_CUDA_TRY(cudaMemcpyAsync(s->d_desc, s->h_desc, sizeof(InstDesc) * n, cudaMemcpyHostToDevice, s->st));
-        PTK_CUDA_TRY(cudaMemcpyAsync(s->d_tile0, s->h_tile0, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s->st));
-        PTK_CUDA_TRY(cudaMemcpyAsync(s->d_face0, s->h_face0, sizeof(long long) * (n + 1), cudaMemcpyHostToDevice,
+    if (n) {   // queued behind the running chunk, which reads the old lists
+        PTK_CUDA_TRY(cudaMemcpyAsync(s->d_desc, h_desc, sizeof(InstDesc) * n, cudaMemcpyHostToDevice, s->st));
+        PTK_CUDA_TRY(cudaMemcpyAsync(s->d_tile0, h_tile0, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s->st));
+        PTK_CUDA_TRY(cudaMemcpyAsync(s->d_face0, h_face0, sizeof(long long) * (n + 1), cudaMemcpyHostToDevice,
                                      s->st));
     }
     s->dirty = false;
@@ -540,7 +592,7 @@ int ptk_server_create(const ptk_server_config *cfg, ptk_server **out)
     }
     if (s->stages && (pool_alloc(sizeof(int), default_stream(), (void **)&s->d_err) ||
                       pool_alloc(sizeof(int) * s->cfg.chunk_steps, default_stream(), (void **)&s->d_work) ||
-                      cudaMallocHost(&s->h_err, sizeof(int)) != cudaSuccess ||
+                      cudaMallocHost(&s->h_err, 2 * sizeof(int)) != cudaSuccess ||
                       cudaMemsetAsync(s->d_err, 0, sizeof(int), default_stream()) != cudaSuccess ||
                       cudaStreamSynchronize(default_stream()) != cudaSuccess)) {
         if (s->d_err) pool_free(s->d_err, default_stream());
@@ -550,16 +602,25 @@ int ptk_server_create(const ptk_server_config *cfg, ptk_server **out)
         delete s;
         return set_error(PTK_ERR_CUDA, "server error word allocation failed");
     }
+    if (s->h_err) s->h_err[0] = s->h_err[1] = 0;
     if (s->cfg.hbm_budget_bytes == 0) {
         size_t f = 0, t = 0;
         cudaMemGetInfo(&f, &t);
         s->cfg.hbm_budget_bytes = f / 10 * 8;
     }
-    if (cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreate(&s->ev[0]) != cudaSuccess || cudaEventCreate(&s->ev[1]) != cudaSuccess) {
-        for (cudaEvent_t e : s->ev)
-            if (e) cudaEventDestroy(e);
+    bool ok = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) == cudaSuccess;
+    for (int b = 0; b < 2 && ok; ++b)
+        ok = cudaEventCreate(&s->ev_start[b]) == cudaSuccess && cudaEventCreate(&s->ev_end[b]) == cudaSuccess &&
+             cudaEventCreateWithFlags(&s->ev_ret[b], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+        for (int b = 0; b < 2; ++b)
+            for (cudaEvent_t e : {s->ev_start[b], s->ev_end[b], s->ev_ret[b]})
+                if (e) cudaEventDestroy(e);
         if (s->st) cudaStreamDestroy(s->st);
+        if (s->d_err) pool_free(s->d_err, default_stream());
+        if (s->d_work) pool_free(s->d_work, default_stream());
+        if (s->h_err) cudaFreeHost(s->h_err);
+        pool_free(s->d_part, default_stream());
         delete s;
         return set_error(PTK_ERR_CUDA, "stream creation failed");
     }
@@ -608,9 +669,30 @@ int ptk_server_run(ptk_server *s, double time_scale)
     s->resident = grid_cap[4];
     auto clock = [&] { return (now_s() - t0); };
     auto arrived = [&](Inst *in, double t) { return time_scale <= 0 || in->t_arrival * time_scale <= t; };
+    // Wait for the chunk of slot b and its retirement copies; complete its finishers.
+    auto land = [&](int b) -> int {
+        ptk_server::Flight &F = s->flight[b];
+        if (!F.on) return PTK_OK;
+        F.on = false;
+        if (cudaEventSynchronize(s->ev_ret[b]) != cudaSuccess)
+            return set_error(PTK_ERR_CUDA, "chunk failed: %s", cudaGetErrorString(cudaGetLastError()));
+        if (s->stages && s->h_err[b])
+            return set_error(PTK_ERR_TIMEOUT, "staged step kernel: a bounded wait expired (error word %d)",
+                             s->h_err[b]);
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, s->ev_start[b], s->ev_end[b]) == cudaSuccess) s->chunk_dev_s += ms * 1e-3;
+        const double t = clock();
+        for (size_t q = 0; q < F.gone.size(); ++q) retire_finish(s, F.gone[q], s->h_sums[b] + 6 * q, t);
+        F.gone.clear();
+        return PTK_OK;
+    };
     int rc = PTK_OK;
-    while ((nxt < order.size() || !s->active.empty()) && rc == PTK_OK) {
+    // One chunk is queued behind the running one: the host admits, rebuilds the work list and
+    // launches chunk i+1 (with chunk i's finishers retired in stream order between them), then
+    // waits for chunk i.
+    while (rc == PTK_OK && (nxt < order.size() || !s->active.empty())) {
         double t = clock();
+        s->up_used[s->par] = 0;   // this half's copies preceded a chunk that has landed
         // admit arrived requests, FIFO, while they fit the budget and the slot limit
         while (nxt < order.size() && arrived(order[nxt], t) && (int)s->active.size() < s->cfg.max_active) {
             Inst *in = order[nxt];
@@ -625,6 +707,15 @@ int ptk_server_run(ptk_server *s, double time_scale)
         }
         if (rc) break;
         if (s->active.empty()) {
+            // nothing to run: complete what is queued, then wait for the next arrival
+            rc = land(s->par ^ 1);
+            if (!rc) rc = land(s->par);
+            if (rc) break;
+            if (cudaStreamSynchronize(s->st) != cudaSuccess) {
+                rc = set_error(PTK_ERR_CUDA, "stream failed: %s", cudaGetErrorString(cudaGetLastError()));
+                break;
+            }
+            s->up_used[0] = s->up_used[1] = 0;
             if (nxt < order.size()) {
                 const double wait = order[nxt]->t_arrival * time_scale - clock();
                 if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.01)));
@@ -643,8 +734,9 @@ int ptk_server_run(ptk_server *s, double time_scale)
         rc = chunk_graph(s, len, grid, &ex);
         if (rc) break;
         s->sched_s += now_s() - ts;
-        if (cudaEventRecord(s->ev[0], s->st) != cudaSuccess || cudaGraphLaunch(ex, s->st) != cudaSuccess ||
-            cudaEventRecord(s->ev[1], s->st) != cudaSuccess) {
+        const int b = s->par;
+        if (cudaEventRecord(s->ev_start[b], s->st) != cudaSuccess || cudaGraphLaunch(ex, s->st) != cudaSuccess ||
+            cudaEventRecord(s->ev_end[b], s->st) != cudaSuccess) {
             rc = set_error(PTK_ERR_CUDA, "chunk launch failed");
             break;
         }
@@ -653,21 +745,12 @@ int ptk_server_run(ptk_server *s, double time_scale)
         count_graph_launch(kernels);
         s->launches += kernels;
         ++s->chunks;
-        if (s->stages && cudaMemcpyAsync(s->h_err, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->st) != cudaSuccess) {
+        if (s->stages &&
+            cudaMemcpyAsync(s->h_err + b, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->st) != cudaSuccess) {
             rc = set_error(PTK_ERR_CUDA, "error word copy failed");
             break;
         }
-        if (cudaStreamSynchronize(s->st) != cudaSuccess) {
-            rc = set_error(PTK_ERR_CUDA, "chunk failed: %s", cudaGetErrorString(cudaGetLastError()));
-            break;
-        }
-        if (s->stages && *s->h_err) {
-            rc = set_error(PTK_ERR_TIMEOUT, "staged step kernel: a bounded wait expired (error word %d)", *s->h_err);
-            break;
-        }
-        float ms = 0;
-        if (cudaEventElapsedTime(&ms, s->ev[0], s->ev[1]) == cudaSuccess) s->chunk_dev_s += ms * 1e-3;
-        t = clock();
+        // This chunk's finishers: checksums (and results) and frees queued behind it.
         const double tr = now_s();
         std::vector<Inst *> still, gone;
         for (Inst *in : s->active) {
@@ -676,32 +759,39 @@ int ptk_server_run(ptk_server *s, double time_scale)
         }
         s->active.swap(still);
         if (!gone.empty()) {
-            // every finisher's checksums and frees in stream order, then one synchronisation
-            if ((int)gone.size() > s->sums_cap) {
-                if (s->h_sums) cudaFreeHost(s->h_sums);
-                s->h_sums = nullptr;
-                s->sums_cap = 0;
-                if (cudaMallocHost(&s->h_sums, sizeof(double) * 6 * gone.size()) != cudaSuccess) {
+            if ((int)gone.size() > s->sums_cap[b]) {
+                // slot b's landing slots were read when slot b last landed
+                if (s->h_sums[b]) cudaFreeHost(s->h_sums[b]);
+                s->h_sums[b] = nullptr;
+                s->sums_cap[b] = 0;
+                if (cudaMallocHost(&s->h_sums[b], sizeof(double) * 6 * gone.size()) != cudaSuccess) {
                     for (Inst *in : gone) release(s, in);
                     rc = set_error(PTK_ERR_NOMEM, "pinned checksum slots");
                     break;
                 }
-                s->sums_cap = (int)gone.size();
+                s->sums_cap[b] = (int)gone.size();
             }
             for (size_t q = 0; q < gone.size(); ++q) {
-                if (!rc) rc = retire_enqueue(s, gone[q], s->h_sums + 6 * q);
+                if (!rc) rc = retire_enqueue(s, gone[q], s->h_sums[b] + 6 * q);
                 else release(s, gone[q]);
             }
             if (rc) break;
-            if (cudaStreamSynchronize(s->st) != cudaSuccess) {
-                rc = set_error(PTK_ERR_CUDA, "retirement failed: %s", cudaGetErrorString(cudaGetLastError()));
-                break;
-            }
-            for (size_t q = 0; q < gone.size(); ++q) retire_finish(s, gone[q], s->h_sums + 6 * q, t);
             s->dirty = true;
         }
+        if (cudaEventRecord(s->ev_ret[b], s->st) != cudaSuccess) {
+            rc = set_error(PTK_ERR_CUDA, "event record failed");
+            break;
+        }
+        s->flight[b].on = true;
+        s->flight[b].gone.swap(gone);
         s->retire_s += now_s() - tr;
+        // the previous chunk ran while this one was prepared
+        rc = land(b ^ 1);
+        s->par = b ^ 1;
     }
+    if (rc == PTK_OK) rc = land(s->par ^ 1);
+    if (rc == PTK_OK) rc = land(s->par);
+    if (rc != PTK_OK) cudaStreamSynchronize(s->st);
     s->wall_s += clock();
     return rc;
 }
@@ -780,18 +870,22 @@ int ptk_server_destroy(ptk_server *s)
     if (s->d_desc) pool_free(s->d_desc, s->st);
     if (s->d_tile0) pool_free(s->d_tile0, s->st);
     if (s->d_face0) pool_free(s->d_face0, s->st);
-    if (s->h_desc) cudaFreeHost(s->h_desc);
-    if (s->h_tile0) cudaFreeHost(s->h_tile0);
-    if (s->h_face0) cudaFreeHost(s->h_face0);
+    for (int b = 0; b < 2; ++b) {
+        if (s->h_desc[b]) cudaFreeHost(s->h_desc[b]);
+        if (s->h_tile0[b]) cudaFreeHost(s->h_tile0[b]);
+        if (s->h_face0[b]) cudaFreeHost(s->h_face0[b]);
+        if (s->h_sums[b]) cudaFreeHost(s->h_sums[b]);
+        if (s->h_up[b]) cudaFreeHost(s->h_up[b]);
+    }
     if (s->d_err) pool_free(s->d_err, s->st);
     if (s->d_work) pool_free(s->d_work, s->st);
     if (s->h_err) cudaFreeHost(s->h_err);
     if (s->d_part) pool_free(s->d_part, s->st);
-    if (s->h_sums) cudaFreeHost(s->h_sums);
     cudaStreamSynchronize(s->st);
     cudaStreamDestroy(s->st);
-    for (cudaEvent_t e : s->ev)
-        if (e) cudaEventDestroy(e);
+    for (int b = 0; b < 2; ++b)
+        for (cudaEvent_t e : {s->ev_start[b], s->ev_end[b], s->ev_ret[b]})
+            if (e) cudaEventDestroy(e);
     for (Inst *in : s->all) delete in;
     delete s;
     return PTK_OK;
