@@ -298,6 +298,15 @@ int ptk_server_fetch(ptk_server *s, long long ticket, float *const fields[6]);
 int ptk_server_stats_get(ptk_server *s, ptk_server_stats *st);
 int ptk_server_destroy(ptk_server *s);
 
+/* ============================== self-test of the bounded waits ================================ */
+/* The staged step kernel waits for its TMA copies on mbarriers for at most 1 s of global time (and
+ * at most 2^22 polls) and, when a wait runs out, raises an error word, lets its copies in flight land and returns; the host
+ * then reports PTK_ERR_TIMEOUT instead of hanging.  This launches one CTA that arms an mbarrier for
+ * 16 bytes of transactions that nothing delivers (no copy is issued) and waits on it with the same
+ * bounded wait.  Returns PTK_ERR_TIMEOUT with *error_word = 1 and *elapsed_ms = the launch's device
+ * time when the wait ran out as designed; the context stays usable.  No reference counterpart. */
+int ptk_selftest_wait_expiry(int *error_word, float *elapsed_ms);
+
 /* ============================== autotuner ===================================================== */
 /* Time candidate tile shapes for a grid of the given size on the current device and return the
  * fastest (cached per shape for the life of the process). */

@@ -139,6 +139,7 @@ _SIGS = {
     "ptk_server_stats_get": (C.c_int, [_P, C.POINTER(ServerStats)]),
     "ptk_server_destroy": (C.c_int, [_P]),
     "ptk_autotune_tiles":(C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(TileConfig), C.POINTER(C.c_float)]),
+    "ptk_selftest_wait_expiry": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_float)]),
     "ptk_problem_generate": (C.c_int, [C.POINTER(ProblemDesc), C.POINTER(FdtdParams), _P, _P, _P, _P,
                                        C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), _P]),
     "ptk_reference_params": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(FdtdParams)]),

@@ -52,7 +52,8 @@ __host__ __device__ constexpr int width_of(int by) { return (by == 7 || by == 23
 // CTAs per SM the instantiation is compiled for: four-warp CTAs (7 rows) run three to an SM, each
 // with its own plane barrier; the others one.
 __host__ __device__ constexpr int ctas_per_sm(int by) { return by == 7 ? 3 : 1; }
-constexpr int kWaitLimit = 1 << 22;
+constexpr int kWaitLimit = 1 << 22;               // polls: a hard cap (about 16 s on GB300)
+constexpr unsigned long long kWaitNs = 1000000000ull;   // the wait gives up after 1 s of global time
 constexpr int kMapMat = 16;     // tensor map of the material index in an instance's set
 constexpr size_t kTabBytes = 256 * sizeof(float4);   // material table (Ca, Cb, Da, Db) per entry
 
@@ -120,10 +121,19 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
                  : "memory");
 }
 
-// Bounded wait for the phase with the given parity to complete.
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait for the phase with the given parity to complete: gives up after kWaitNs of global
+// time (read only once a poll has come back empty) or kWaitLimit polls, whichever comes first.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
 {
     const uint32_t a = smem_u32(bar);
+    unsigned long long t0 = 0;
     for (int it = 0; it < kWaitLimit; ++it) {
         uint32_t done;
         asm volatile(
@@ -134,6 +144,8 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
             : "r"(a), "r"(parity)
             : "memory");
         if (done) return true;
+        if (it == 0) t0 = global_ns();
+        else if ((it & 15) == 0 && global_ns() - t0 > kWaitNs) return false;
     }
     return false;
 }
@@ -685,6 +697,61 @@ int yee_bulk_resident_ctas(int by, int stages, bool mat)
 #undef PTK_RES
     return 0;
 }
+
+// ---------------------------------------------------------------------------------------------
+// Self-test of the bounded wait: an mbarrier armed for transactions that never arrive.
+// ---------------------------------------------------------------------------------------------
+__global__ void k_wait_expiry_probe(int *err)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) mbar_expect_tx(&bar, 16);   // the phase needs 16 bytes that no copy brings
+    __syncthreads();
+    if (!mbar_wait(&bar, 0) && threadIdx.x == 0) atomicOr(err, 1);
+}
+
+}  // namespace ptk
+
+extern "C" int ptk_selftest_wait_expiry(int *error_word, float *elapsed_ms)
+{
+    using namespace ptk;
+    clear_error();
+    int rc = ensure_init();
+    if (rc) return rc;
+    cudaStream_t st = default_stream();
+    int *d_err = nullptr;
+    rc = pool_alloc(sizeof(int), st, (void **)&d_err);
+    if (rc) return rc;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaMemsetAsync(d_err, 0, sizeof(int), st);
+    cudaEventRecord(e0, st);
+    k_wait_expiry_probe<<<1, 32, 0, st>>>(d_err);
+    const cudaError_t le = cudaGetLastError();
+    count_launches(1);
+    cudaEventRecord(e1, st);
+    int h = 0;
+    cudaMemcpyAsync(&h, d_err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    const cudaError_t se = cudaStreamSynchronize(st);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    pool_free(d_err, st);
+    if (le != cudaSuccess || se != cudaSuccess)
+        return set_error(PTK_ERR_CUDA, "wait-expiry probe failed: %s", cudaGetErrorString(le != cudaSuccess ? le : se));
+    if (error_word) *error_word = h;
+    if (elapsed_ms) *elapsed_ms = ms;
+    if (h) return set_error(PTK_ERR_TIMEOUT, "bounded wait expired after %.1f ms (error word %d)", ms, h);
+    return set_error(PTK_ERR_STATE, "the probe's wait completed, but no transaction could complete it");
+}
+
+namespace ptk {
 
 // ---------------------------------------------------------------------------------------------
 // Tensor maps.

@@ -392,3 +392,27 @@ def test_staged_full_size_matches_register_kernel(full_problem):
     for o in outs[1:]:
         for a, b in zip(outs[0], o):
             np.testing.assert_array_equal(a, b)
+
+
+# ------------------------------------------------------------------------------------------------
+# Bounded waits: a wait that cannot complete runs out, reports, and leaves the context usable.
+# ------------------------------------------------------------------------------------------------
+def test_bounded_wait_runs_out_and_context_stays_usable():
+    word, ms = C.c_int(-1), C.c_float(-1)
+    rc = _lib.lib().ptk_selftest_wait_expiry(C.byref(word), C.byref(ms))
+    assert rc == 5, _lib.lib().ptk_last_error()          # PTK_ERR_TIMEOUT
+    assert word.value == 1
+    assert 0 < ms.value < 30000, ms.value                # the poll limit ends the wait within seconds
+    assert b"bounded wait expired" in _lib.lib().ptk_last_error()
+    # the same process still solves bit for bit
+    shape, steps = (40, 33, 17), 6
+    pr = P.Problem.generate(*shape, n_boxes=2, eps=(1, 6), box=(4, 12), steps=steps, seed=31)
+    f = P.random_fields(*shape, seed=75, scale=1e-2)
+    with P.Solver(pr.params) as s:
+        s.set_tiles(11, 0, 4, 4)
+        s.set_fields(f)
+        s.set_problem(pr)
+        s.run(steps)
+        got = s.get_fields()
+    assert_parity(got, oracle.step_ext_f32(f, steps, pr.params, pr.Ca, pr.Cb, pr.Da, pr.Db, pr.src, pr.wave),
+                  "solve after an expired wait")
