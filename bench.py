@@ -341,6 +341,34 @@ def run_ours(args, wl, world, rank, local):
         e2e_step(record=True)
     result_ok = bool(np.isfinite(hout[5].array).all() and np.abs(hout[5].array).max() > 0)
 
+    # ---- the reference-facing path: the PTask FDTD graph with host buffers ---------------------------
+    # Cyclic graph (MF_GENERAL_ITERATOR loop, lowered to the fused step): per bench step, push the
+    # coefficients and the source (set_problem), push the six fields, run the iteration and pull the
+    # six fields, as the reference's driver does with its unrolled graph (graphfdtd.cpp:1076-1125).
+    graph_e2e = None
+    if not args.no_graph_e2e:
+        from ptask_gb300.graph import FDTDGraph
+        with FDTDGraph(prob.params, "fused") as g:
+            def graph_step():
+                g.set_problem(prob)
+                return g.solve(zero, T)
+
+            for _ in range(max(1, args.warmup)):
+                gout = graph_step()
+            dist.barrier()
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                gout = graph_step()
+            g_s = dist.max(time.perf_counter() - t0)
+            gst = g.stats()
+        graph_e2e = {
+            "value": cells * T * args.steps * world / g_s / 1e6, "unit": "Mcell-updates/s",
+            "ms_per_step": g_s * 1e3 / args.steps, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "path": "PTask graph API (ptk_fdtd_graph_set_problem + ptk_fdtd_graph_solve: Push, Graph::Run of "
+                    "the cyclic FDTD graph lowered to the fused step, Pull), pageable host arrays",
+            "same_result_as_solver_path": all(np.array_equal(a, h.array) for a, h in zip(gout, hout)),
+            "cycles_lowered": gst["cycles_lowered"]}
+
     total_cell_updates = cells * T * args.steps * world
     value = total_cell_updates / (dev_ms / 1e3) / 1e6
     e2e_value = total_cell_updates / e2e_s / 1e6
@@ -374,6 +402,7 @@ def run_ours(args, wl, world, rank, local):
                      "algorithmic_bytes_per_cell": bpc,
                      "frac_of_64B_cell_traffic": BYTES_PER_CELL * cells / (per_launch_ms / 1e3) / 1e9 / peak,
                      "launch_ms": per_launch_ms},
+        "e2e_graph": graph_e2e,
         "e2e": {"value": e2e_value, "unit": "Mcell-updates/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3 / args.steps, "result_ok": result_ok,
                 "phases_ms_per_step": {k: v / args.steps for k, v in phase_ms.items()}},
@@ -482,6 +511,8 @@ def main() -> int:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--dense-coefficients", action="store_true",
                     help="read the four per-cell coefficient arrays instead of the material index")
+    ap.add_argument("--no-graph-e2e", action="store_true",
+                    help="plain workloads: skip the end-to-end run through the PTask graph API")
     ap.add_argument("--no-plain-graph", action="store_true",
                     help="batched/served: skip the per-graph (task-wise) plain dispatch arm")
     args = ap.parse_args()

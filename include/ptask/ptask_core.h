@@ -443,6 +443,11 @@ private:
     std::string m_xml_error;
 };
 
+// Host copy of `bytes`, split over the host cores when it is large (one core moves a few tens of
+// GB/s; the fields of one FDTD solve are about a gigabyte).  Used for datablock initial data and
+// for Pull results.
+void HostCopy(void *dst, const void *src, size_t bytes);
+
 // ---------------------------------------------------------------------------------------------
 // The single CUDA accelerator this runtime drives (accelerator.h).
 class Accelerator {

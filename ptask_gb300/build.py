@@ -102,8 +102,8 @@ def build_runtime(verbose: bool = False) -> Path | None:
         obj = BUILD / ("rt_" + src.stem + ".o")
         objs.append(obj)
         if _newer(obj, [src] + hdrs):
-            jobs.append(["g++"] + CXX_FLAGS + ["-I", str(INCLUDE / "ptask"), "-pthread", "-c", str(src),
-                         "-o", str(obj)])
+            jobs.append(["g++"] + CXX_FLAGS + ["-I", str(INCLUDE / "ptask"), "-pthread", "-fopenmp", "-c",
+                         str(src), "-o", str(obj)])
     with ThreadPoolExecutor(max_workers=max(2, min(8, os.cpu_count() or 2))) as ex:
         for f in [ex.submit(_run, c) for c in jobs]:
             f.result()
@@ -111,7 +111,7 @@ def build_runtime(verbose: bool = False) -> Path | None:
     core = BUILD / "libptask_gb300.so"
     if jobs or _newer(lib, objs + [core]):
         _run(["g++", "-shared", "-o", str(lib)] + [str(o) for o in objs] +
-             ["-L", str(BUILD), "-lptask_gb300", "-pthread", "-ldl", "-Wl,-rpath,$ORIGIN"])
+             ["-L", str(BUILD), "-lptask_gb300", "-pthread", "-fopenmp", "-ldl", "-Wl,-rpath,$ORIGIN"])
     bindir = BUILD / "bin"
     bindir.mkdir(exist_ok=True)
     jobs = []

@@ -8,7 +8,9 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <unordered_map>
 
 namespace ptk {
 
@@ -178,18 +180,57 @@ int ptk_mem_free(void *dptr, void *stream)
     return pool_free(dptr, S(stream));
 }
 
+// Pinned host memory: the driver page-locks every allocation, milliseconds for the tens of
+// megabytes of one field, and a graph pushes and pulls fresh datablocks every solve.  Freed buffers
+// are therefore kept by exact size and handed out again (the host half of the reference's block
+// pools, ptask/BlockPool.cpp); at most kHostCacheBytes are held, the rest is returned to the driver.
+// Callers free a buffer only after their copies from or into it have completed.
+namespace {
+constexpr size_t kHostCacheBytes = (size_t)4 << 30;
+std::mutex g_host_mu;
+std::multimap<size_t, void *> g_host_cache;      // free buffers by size
+std::unordered_map<void *, size_t> g_host_size;  // every buffer handed out or cached
+size_t g_host_cached = 0;
+}  // namespace
+
 int ptk_host_alloc(size_t bytes, void **hptr)
 {
     int rc = ensure_init();
     if (rc) return rc;
     PTK_CHECK_ARG(hptr, "hptr is NULL");
-    PTK_CUDA_TRY(cudaMallocHost(hptr, bytes ? bytes : 16));
+    if (!bytes) bytes = 16;
+    {
+        std::lock_guard<std::mutex> lk(g_host_mu);
+        auto it = g_host_cache.find(bytes);
+        if (it != g_host_cache.end()) {
+            *hptr = it->second;
+            g_host_cache.erase(it);
+            g_host_cached -= bytes;
+            return PTK_OK;
+        }
+    }
+    PTK_CUDA_TRY(cudaMallocHost(hptr, bytes));
+    std::lock_guard<std::mutex> lk(g_host_mu);
+    g_host_size[*hptr] = bytes;
     return PTK_OK;
 }
 
 int ptk_host_free(void *hptr)
 {
     if (!hptr) return PTK_OK;
+    {
+        std::lock_guard<std::mutex> lk(g_host_mu);
+        auto it = g_host_size.find(hptr);
+        if (it != g_host_size.end()) {
+            const size_t b = it->second;
+            if (g_host_cached + b <= kHostCacheBytes) {
+                g_host_cache.emplace(b, hptr);
+                g_host_cached += b;
+                return PTK_OK;
+            }
+            g_host_size.erase(it);
+        }
+    }
     PTK_CUDA_TRY(cudaFreeHost(hptr));
     return PTK_OK;
 }

@@ -110,9 +110,13 @@ class FDTDGraph:
                                                int(self._wave.size)), "set_problem")
 
     def solve(self, fields, steps: int) -> list[np.ndarray]:
-        out = [np.array(f, np.float32, copy=True, order="C") for f in fields]
-        ptrs = (C.c_void_p * 6)(*[a.ctypes.data for a in out])
-        _check(rt().ptk_fdtd_graph_solve(self._h, ptrs, steps), "ptk_fdtd_graph_solve")
+        """Push the six fields, run `steps` iterations, pull the results into new arrays (the
+        inputs are left as they are)."""
+        ins = [np.ascontiguousarray(f, np.float32) for f in fields]
+        out = [np.empty_like(a) for a in ins]
+        _check(rt().ptk_fdtd_graph_solve_many(self._h, (C.c_void_p * 6)(*[a.ctypes.data for a in ins]), 1,
+                                              (C.c_void_p * 6)(*[a.ctypes.data for a in out]), steps),
+               "ptk_fdtd_graph_solve")
         return out
 
     def solve_many(self, fields, instances: int, steps: int) -> list[list[np.ndarray]]:

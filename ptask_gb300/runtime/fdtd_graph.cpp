@@ -457,7 +457,7 @@ static int solve_impl(ptk_fdtd_graph *G, float *const fields[6], int instances, 
             b->Lock();
             const void *src = b->GetDataPointer(FALSE);
             float *dst = results ? results[inst * 6 + f] : fields[f];
-            memcpy(dst, src, bytes[f]);
+            HostCopy(dst, src, bytes[f]);
             b->Unlock();
             b->Release();
         }

@@ -2,8 +2,10 @@
 // resolution for the GB300 runtime.  Device work goes through the C ABI of libptask_gb300.so.
 #include <dlfcn.h>
 
+#include <algorithm>
 #include <cstdarg>
 #include <cstdlib>
+#include <cstring>
 #include <map>
 #include <mutex>
 
@@ -254,6 +256,21 @@ size_t Accelerator::GetGlobalMemorySize()
     return t;
 }
 
+void HostCopy(void *dst, const void *src, size_t bytes)
+{
+    constexpr size_t kPiece = (size_t)4 << 20;
+    if (bytes < 4 * kPiece) {
+        memcpy(dst, src, bytes);
+        return;
+    }
+    const long long n = (long long)((bytes + kPiece - 1) / kPiece);
+#pragma omp parallel for schedule(static)
+    for (long long c = 0; c < n; ++c) {
+        const size_t o = (size_t)c * kPiece;
+        memcpy(static_cast<char *>(dst) + o, static_cast<const char *>(src) + o, std::min(kPiece, bytes - o));
+    }
+}
+
 namespace Runtime {
 
 PTRESULT Initialize()
@@ -366,7 +383,7 @@ Datablock *AllocateDatablock(DatablockTemplate *t, void *init, UINT cb, Channel 
     if (init) {
         char *h = (char *)b->GetDataPointer(TRUE, FALSE);
         if (cb >= bytes) {
-            memcpy(h, init, bytes);
+            HostCopy(h, init, bytes);
         } else {
             for (size_t i = 0; i < bytes; i += cb) memcpy(h + i, init, std::min<size_t>(cb, bytes - i));
         }
