@@ -89,7 +89,11 @@ int ptk_kernel_signature(int kernel_id, int *n_inputs, int *n_outputs, int *cons
 
 int ptk_mem_alloc(size_t bytes, void *stream, void **dptr);
 int ptk_mem_free(void *dptr, void *stream);
-int ptk_host_alloc(size_t bytes, void **hptr);              /* pinned host memory */
+/* Pinned host memory.  Freed buffers are kept, by exact size, for the next allocation of that size
+ * (page-locking tens of megabytes takes milliseconds); at most 4 GiB stay cached for the life of
+ * the process, beyond that buffers go back to the driver.  Free a buffer only after the copies
+ * from or into it have completed. */
+int ptk_host_alloc(size_t bytes, void **hptr);
 int ptk_host_free(void *hptr);
 int ptk_memcpy_h2d(void *dst, const void *src, size_t bytes, void *stream);
 int ptk_memcpy_d2h(void *dst, const void *src, size_t bytes, void *stream);
