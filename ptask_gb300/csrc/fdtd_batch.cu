@@ -154,7 +154,6 @@ struct ptk_server {
     cudaStream_t st = nullptr;
     std::vector<Inst *> all;        // every submitted request, by ticket
     std::vector<Inst *> active;     // admitted, running
-    size_t next = 0;                // next request to admit (arrival order)
     size_t used = 0, peak_bytes = 0;
     int peak_active = 0;
     // device work list; its pinned host staging is double-buffered by `par` (below)
@@ -194,7 +193,6 @@ struct ptk_server {
     double chunk_dev_s = 0, admit_s = 0, retire_s = 0, sched_s = 0;   // where wall_s went
     cudaEvent_t ev_start[2] = {}, ev_end[2] = {};   // around each chunk replay, per slot
     cudaEvent_t ev_ret[2] = {};                      // after the slot's retirement copies
-    double t0_wall = 0;
     std::mutex mu;
 };
 
@@ -662,11 +660,11 @@ int ptk_server_run(ptk_server *s, double time_scale)
     for (Inst *in : order) in->t_arrival_run = time_scale > 0 ? in->t_arrival * time_scale : 0.0;
     const double t0 = now_s();
     size_t nxt = 0;
-    int grid_cap[5] = {0, 0, 0, 0, 0};   // resident CTAs per vec (1, 2, 4)
+    int grid_cap[5] = {0, 0, 0, 0, 0};   // resident CTAs of the step kernel per vec (1, 2, 4)
     for (int v : {1, 2, 4})
         grid_cap[v] = std::max(1, s->stages ? yee_bulk_resident_ctas(s->rows, s->stages, true)
                                             : yee_resident_ctas(s->rows, v));
-    s->resident = grid_cap[4];
+    s->resident = grid_cap[s->vec];
     auto clock = [&] { return (now_s() - t0); };
     auto arrived = [&](Inst *in, double t) { return time_scale <= 0 || in->t_arrival * time_scale <= t; };
     // Wait for the chunk of slot b and its retirement copies; complete its finishers.

@@ -95,8 +95,6 @@ int build_material_index(const float *const coef[4], const Layout &L, unsigned c
 // memory (kTmaSetBytes).
 int encode_tma_set(const InstDesc &d, int by, void *host_out);
 
-// Shape of the fused step kernel's main tiles (x width is fixed at 128 cells).
-constexpr int kTileX = 128;
 constexpr int kFaceCellsPerThread = 4;
 
 // Work-list geometry for an instance under tile rows `by`, depth `kc` and `vec` x cells per thread
