@@ -30,10 +30,13 @@
 #include <mutex>
 
 #include "fdtd_device.cuh"
+#include "fdtd_tma.cuh"
 
 namespace ptk {
 
 namespace {
+
+using namespace tma;
 
 // Tile width W (cells): 128 (a warp per row, 4 cells per lane) or 64 (a warp per two rows, 16
 // lanes per row).  A staged float row covers x0-4 .. x0+W+3 and a material-index row x0-16 ..
@@ -52,10 +55,7 @@ __host__ __device__ constexpr int width_of(int by) { return (by == 7 || by == 23
 // CTAs per SM the instantiation is compiled for: four-warp CTAs (7 rows) run three to an SM, each
 // with its own plane barrier; the others one.
 __host__ __device__ constexpr int ctas_per_sm(int by) { return by == 7 ? 3 : 1; }
-constexpr int kWaitLimit = 1 << 22;               // polls: a hard cap (about 16 s on GB300)
-constexpr unsigned long long kWaitNs = 1000000000ull;   // the wait gives up after 1 s of global time
 constexpr int kMapMat = 16;     // tensor map of the material index in an instance's set
-constexpr size_t kTabBytes = 256 * sizeof(float4);   // material table (Ca, Cb, Da, Db) per entry
 
 // Arrays in stage order and the frame rows r (j = y0 - 1 + r) each one needs.  With per-cell
 // coefficient arrays the stage holds Ca, Cb, Da, Db; with a material index (MAT) one byte per
@@ -106,71 +106,6 @@ template <int BY, int S, bool MAT>
 __host__ __device__ constexpr size_t smem_bytes()
 {
     return S * stage_bytes<BY, MAT>() + xchg_bytes<BY>() + (MAT ? kTabBytes : 0) + S * 8 + 16;
-}
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ unsigned long long global_ns()
-{
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-// Bounded wait for the phase with the given parity to complete: gives up after kWaitNs of global
-// time (read only once a poll has come back empty) or kWaitLimit polls, whichever comes first.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
-{
-    const uint32_t a = smem_u32(bar);
-    unsigned long long t0 = 0;
-    for (int it = 0; it < kWaitLimit; ++it) {
-        uint32_t done;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(a), "r"(parity)
-            : "memory");
-        if (done) return true;
-        if (it == 0) t0 = global_ns();
-        else if ((it & 15) == 0 && global_ns() - t0 > kWaitNs) return false;
-    }
-    return false;
-}
-
-__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-        "[%5];" ::"r"(smem_u32(dst)),
-        "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
-        : "memory");
-}
-
-__device__ __forceinline__ void tma_acquire(const CUtensorMap *map)
-{
-    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(map) : "memory");
-}
-
-__device__ __forceinline__ float4 ld4s(const float *p) { return *reinterpret_cast<const float4 *>(p); }
-
-__device__ __forceinline__ float yee_b(float d, float h, float c, float a1, float a0, float s1, float b1, float b0,
-                                       float s2)
-{
-    const float curl = __fsub_rn(__fmul_rn(__fsub_rn(a1, a0), s1), __fmul_rn(__fsub_rn(b1, b0), s2));
-    return __fadd_rn(__fmul_rn(d, h), __fmul_rn(c, curl));
 }
 
 // Map of array a for field parity par in an instance's map set.
@@ -756,7 +691,7 @@ namespace ptk {
 // ---------------------------------------------------------------------------------------------
 // Tensor maps.
 // ---------------------------------------------------------------------------------------------
-static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 {
     static std::once_flag once;
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -774,7 +709,7 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
 template <int BY>
 static int encode_set(const InstDesc &d, CUtensorMap *out)
 {
-    PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
     if (!enc) return set_error(PTK_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
     const cuuint64_t dims[3] = {(cuuint64_t)d.pitch, (cuuint64_t)d.ny + 1, (cuuint64_t)d.nz + 1};
     const cuuint64_t strides[2] = {(cuuint64_t)d.pitch * 4, (cuuint64_t)d.plane * 4};
