@@ -122,6 +122,10 @@ public:
     void *DeviceView(void *stream, bool for_write, bool keep_contents);   // device pointer, valid on `stream`
     void DeviceWritten(void *stream);                                      // a kernel on `stream` wrote it
     void StartHostMaterialization(void *stream);                           // EAGER: async D2H
+    // Whole-block copies straight between caller memory (pinned or not) and the device view, with
+    // no host view in between: for blocks that live on the device (pushed fields, pulled results).
+    void UploadFrom(const void *src);     // pageable src: reusable on return; pinned: once consumed
+    void DownloadTo(void *dst);           // from the host view if it is (being) materialised
     const void *HostBytes();                                               // host copy without syncing (params)
     size_t Bytes() const { return m_bytes; }
 

@@ -109,11 +109,16 @@ class FDTDGraph:
                                                self._wave.ctypes.data if self._wave.size else None,
                                                int(self._wave.size)), "set_problem")
 
-    def solve(self, fields, steps: int) -> list[np.ndarray]:
-        """Push the six fields, run `steps` iterations, pull the results into new arrays (the
-        inputs are left as they are)."""
+    def solve(self, fields, steps: int, out: list[np.ndarray] | None = None) -> list[np.ndarray]:
+        """Push the six fields, run `steps` iterations, pull the results into `out` (six C-contiguous
+        float32 arrays of the fields' shapes, reused across calls) or into new arrays.  The inputs
+        are left as they are."""
         ins = [np.ascontiguousarray(f, np.float32) for f in fields]
-        out = [np.empty_like(a) for a in ins]
+        if out is None:
+            out = [np.empty_like(a) for a in ins]
+        elif len(out) != 6 or any(o.shape != a.shape or o.dtype != np.float32 or not o.flags.c_contiguous
+                                  for o, a in zip(out, ins)):
+            raise ValueError("out must be six C-contiguous float32 arrays shaped like the fields")
         _check(rt().ptk_fdtd_graph_solve_many(self._h, (C.c_void_p * 6)(*[a.ctypes.data for a in ins]), 1,
                                               (C.c_void_p * 6)(*[a.ctypes.data for a in out]), steps),
                "ptk_fdtd_graph_solve")

@@ -439,8 +439,10 @@ static int solve_impl(ptk_fdtd_graph *G, float *const fields[6], int instances, 
     for (int inst = 0; inst < instances; ++inst) {
         for (int f = 0; f < 6; ++f) {
             // One block per field, pushed into every channel that reads it (graphfdtd.cpp:1078-1096).
-            Datablock *b = Runtime::AllocateDatablock(G->field_t[f], fields[f], (UINT)bytes[f], G->field_in[f][0]);
+            // The fields are read on the device only: they go straight to the block's device view.
+            Datablock *b = Runtime::AllocateDatablock(G->field_t[f], nullptr, 0, G->field_in[f][0]);
             if (!b) return PTK_ERR_NOMEM;
+            b->UploadFrom(fields[f]);
             for (GraphInputChannel *c : G->field_in[f]) c->Push(b);
             b->Release();
         }
@@ -454,11 +456,7 @@ static int solve_impl(ptk_fdtd_graph *G, float *const fields[6], int instances, 
         for (int f = 0; f < 6; ++f) {
             Datablock *b = G->field_out[f]->Pull();
             if (!b) return PTK_ERR_TIMEOUT;
-            b->Lock();
-            const void *src = b->GetDataPointer(FALSE);
-            float *dst = results ? results[inst * 6 + f] : fields[f];
-            HostCopy(dst, src, bytes[f]);
-            b->Unlock();
+            b->DownloadTo(results ? results[inst * 6 + f] : fields[f]);
             b->Release();
         }
     G->last_solve_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();

@@ -223,6 +223,55 @@ void Datablock::DeviceWritten(void *stream)
     m_d2h_pending = false;
 }
 
+void Datablock::UploadFrom(const void *src)
+{
+    std::lock_guard<std::recursive_mutex> lk(m_lock);
+    void *io = runtime_io_stream();
+    if (!m_dev) {
+        if (ptk_mem_alloc(m_bytes ? m_bytes : 16, io, &m_dev) != PTK_OK) {
+            Runtime::HandleError("%s: device allocation of %zu bytes failed: %s", __FUNCTION__, m_bytes,
+                                 ptk_last_error());
+            return;
+        }
+        m_dev_stream = io;
+    }
+    if (m_dev_stream != io && m_event) ptk_stream_wait_event(io, m_event);
+    // A pageable source is staged by the driver before the call returns; a pinned one is read by
+    // the copy engine, so the event below is what a caller reusing it would wait for.
+    if (ptk_memcpy_h2d(m_dev, src, m_bytes, io) != PTK_OK) {
+        Runtime::HandleError("%s: host-to-device copy failed: %s", __FUNCTION__, ptk_last_error());
+        return;
+    }
+    if (!m_event) ptk_event_create(&m_event);
+    ptk_event_record(m_event, io);
+    m_dev_stream = io;
+    m_dev_valid = true;
+    m_host_valid = false;
+    m_d2h_pending = false;
+}
+
+void Datablock::DownloadTo(void *dst)
+{
+    std::lock_guard<std::recursive_mutex> lk(m_lock);
+    if (m_d2h_pending) {
+        ptk_event_sync(m_event);
+        m_d2h_pending = false;
+        m_host_valid = true;
+    }
+    if (m_host_valid) {
+        HostCopy(dst, m_host, m_bytes);
+        return;
+    }
+    if (!m_dev_valid) {
+        memset(dst, 0, m_bytes);
+        return;
+    }
+    void *io = runtime_io_stream();
+    if (m_event) ptk_stream_wait_event(io, m_event);
+    if (ptk_memcpy_d2h(dst, m_dev, m_bytes, io) != PTK_OK || ptk_stream_sync(io) != PTK_OK)
+        Runtime::HandleError("%s: device-to-host copy failed: %s", __FUNCTION__, ptk_last_error());
+}
+
 void Datablock::StartHostMaterialization(void *stream)
 {
     std::lock_guard<std::recursive_mutex> lk(m_lock);
