@@ -178,15 +178,23 @@ def cpu_sample(prob, shape, target_s: float = 10.0):
     t0 = time.perf_counter()
     oracle.step_ext_f32(f, 2, prob.params, prob.Ca, prob.Cb, prob.Da, prob.Db, prob.src, prob.wave)
     one = (time.perf_counter() - t0) / 2
-    steps = max(1, min(prob.wave.size or 1000, int(target_s / max(one, 1e-6))))
+    total = prob.wave.size or 1000
+    want = max(1, int(target_s / max(one, 1e-6)))
+    steps = min(total, want)
+    # a workload shorter than the target is solved again from its initial fields until the sample
+    # reaches the target time
+    repeats = max(1, min(10000, want // total)) if want > total else 1
     t0 = time.perf_counter()
-    oracle.step_ext_f32(f, steps, prob.params, prob.Ca, prob.Cb, prob.Da, prob.Db, prob.src, prob.wave)
+    for _ in range(repeats):
+        oracle.step_ext_f32(f, steps, prob.params, prob.Ca, prob.Cb, prob.Da, prob.Db, prob.src, prob.wave)
     dt = time.perf_counter() - t0
     cells = shape[0] * shape[1] * shape[2]
-    return {"value": cells * steps / dt / 1e6, "unit": "Mcell-updates/s", "cores": oracle.threads(),
+    what = (f"the whole solve ({steps} steps) {repeats} times" if repeats > 1 else
+            f"first {steps} of the workload's time steps")
+    return {"value": cells * steps * repeats / dt / 1e6, "unit": "Mcell-updates/s", "cores": oracle.threads(),
             "kind": "port",
-            "sample": f"{shape[0]}x{shape[1]}x{shape[2]} grid, first {steps} of the workload's time steps "
-                      f"({dt:.1f} s), oracle/fdtd_oracle.c FP32 with OpenMP"}
+            "sample": f"{shape[0]}x{shape[1]}x{shape[2]} grid, {what} ({dt:.1f} s), oracle/fdtd_oracle.c FP32 "
+                      f"with OpenMP"}
 
 
 def run_reference(args, wl, world, rank, local):
