@@ -495,6 +495,12 @@ def run_served(args, kind, world, rank, local):
             "p50_latency_s": pgraph["p50_latency_s"], "p99_latency_s": pgraph["p99_latency_s"],
             "wall_s": pgraph["wall_s"]},
         "speedup_vs_plain_graph": None if pgraph is None else (len(reqs) / wall) / (pgraph["solves"] / pgraph["wall_s"]),
+        "roofline": {"bound": "hbm", "unit": "GB/s", "peak": hbm_peak()[0], "peak_source": hbm_peak()[1],
+                     "achieved": BYTES_PER_CELL_MAT * cells / best["chunk_device_s"] / 1e9,
+                     "frac": BYTES_PER_CELL_MAT * cells / best["chunk_device_s"] / 1e9 / hbm_peak()[0],
+                     "traffic": None,
+                     "basis": "whole request set: 49 algorithmic bytes per cell update (material index) over the "
+                              "device time of the replayed chunks (all step launches, faces, advances)"},
         "gpu_launches": int(best["launches"]),
         "clocks": clk,
     }
