@@ -416,3 +416,18 @@ def test_bounded_wait_runs_out_and_context_stays_usable():
         got = s.get_fields()
     assert_parity(got, oracle.step_ext_f32(f, steps, pr.params, pr.Ca, pr.Cb, pr.Da, pr.Db, pr.src, pr.wave),
                   "solve after an expired wait")
+
+
+def test_pinned_host_buffers_are_reused_by_size():
+    lib = _lib.lib()
+    a, b, c = C.c_void_p(), C.c_void_p(), C.c_void_p()
+    n = 3 * 1024 * 1024 + 12   # a size nothing else in the process allocates
+    assert lib.ptk_host_alloc(n, C.byref(a)) == 0
+    C.memset(a, 7, n)
+    assert lib.ptk_host_free(a) == 0
+    assert lib.ptk_host_alloc(n, C.byref(b)) == 0
+    assert b.value == a.value                       # the freed buffer came back
+    assert lib.ptk_host_alloc(n, C.byref(c)) == 0   # a second one of the same size is a new buffer
+    assert c.value != b.value
+    for p in (b, c):
+        assert lib.ptk_host_free(p) == 0
