@@ -154,9 +154,12 @@ def hbm_peak():
     return FALLBACK_HBM_GBS, "fallback"
 
 
-def traffic_per_cell(kernel: str, mat: bool = False):
-    """DRAM bytes per cell update of the given fused step kernel from its committed ncu summary."""
+def traffic_per_cell(kernel: str, mat: bool = False, rows: int = 0):
+    """DRAM bytes per cell update of the given fused step kernel from its committed ncu summary (the
+    64-wide 23-row tiles have their own; other staged shapes use the 11-row figure)."""
     name = {("k_yee_step_bulk", True): "yee_step_bulk_mat_256.md", ("k_yee_step_bulk", False): "yee_step_bulk_256.md"}
+    if kernel == "k_yee_step_bulk" and mat and rows == 23:
+        name[(kernel, mat)] = "yee_step_bulk_mat23_256.md"
     f = ROOT / "profiles" / name.get((kernel, mat), "yee_step_256.md")
     if not f.exists():
         return None
@@ -388,7 +391,7 @@ def run_ours(args, wl, world, rank, local):
     achieved = bpc * cells / (per_launch_ms / 1e3) / 1e9
     by, kc, vec, stages = solver.tiles()
     kernel = "k_yee_step_bulk" if run_stages else "k_yee_step"
-    tpc = traffic_per_cell(kernel, mat)
+    tpc = traffic_per_cell(kernel, mat, by)
     line = {
         "metric": "FDTD Mcell-updates/s", "value": value, "unit": "Mcell-updates/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
@@ -456,9 +459,11 @@ def run_served(args, kind, world, rank, local):
             for r in reqs:
                 s.submit(r)
             l0 = P.launch_count()
+            t0 = _lib.lib().ptk_pool_trim_count()
             s.run(time_scale=scale)
             st = s.stats()
             st["launches"] = P.launch_count() - l0
+            st["pool_trims"] = _lib.lib().ptk_pool_trim_count() - t0
             return st
 
     for _ in range(args.warmup if kind == "batched" else 0):
@@ -482,7 +487,7 @@ def run_served(args, kind, world, rank, local):
         "p50_latency_s": best["p50_latency_s"], "p99_latency_s": best["p99_latency_s"],
         "peak_active": best["peak_active"], "peak_bytes": best["peak_bytes"],
         "wall_breakdown_s": {k: best[k] for k in ("wall_s", "chunk_device_s", "admit_s", "retire_s", "schedule_s")},
-        "chunks": best["chunks"], "graph_captures": best["graph_captures"],
+        "chunks": best["chunks"], "graph_captures": best["graph_captures"], "pool_trims": best["pool_trims"],
         "plain": {"solves_per_s": len(reqs) / plain["wall_s"], "mcell_updates_per_s": cells / plain["wall_s"] / 1e6,
                   "p50_latency_s": plain["p50_latency_s"], "p99_latency_s": plain["p99_latency_s"],
                   "wall_s": plain["wall_s"]},

@@ -111,6 +111,9 @@ int ptk_stream_wait_event(void *stream, void *event);
 int ptk_event_elapsed_ms(void *start, void *stop, float *ms);
 /* Bytes currently reserved by the runtime's device pool. */
 int ptk_pool_stats(size_t *reserved_bytes, size_t *used_bytes);
+/* Allocations that failed, found the pool's cached free blocks fragmented, trimmed the cache back
+ * to the driver (after the queued frees ran) and succeeded or failed on the retry. */
+long long ptk_pool_trim_count(void);
 /* Kernel launches issued by this library since load (each CUDA-graph replay adds its node count). */
 long long ptk_launch_count(void);
 

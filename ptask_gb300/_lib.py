@@ -98,6 +98,7 @@ _SIGS = {
     "ptk_stream_wait_event": (C.c_int, [_P, _P]),
     "ptk_event_elapsed_ms": (C.c_int, [_P, _P, C.POINTER(C.c_float)]),
     "ptk_pool_stats": (C.c_int, [C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
+    "ptk_pool_trim_count": (C.c_longlong, []),
     "ptk_launch_count": (C.c_longlong, []),
     "ptk_launch_field_update": (C.c_int, [C.c_int, _P, _P, _P, C.POINTER(FdtdParams), _P, _P]),
     "ptk_launch_h_half_step": (C.c_int, [C.POINTER(_P), C.POINTER(_P), C.POINTER(FdtdParams), _P]),

@@ -22,6 +22,7 @@ static int g_sms = 0;
 static cudaStream_t g_stream = nullptr;
 static cudaMemPool_t g_pool = nullptr;
 static std::atomic<long long> g_launches{0};
+static std::atomic<long long> g_trims{0};   // pool trims after a failed allocation
 
 int set_error(int code, const char *fmt, ...)
 {
@@ -92,6 +93,16 @@ int pool_alloc(size_t bytes, cudaStream_t s, void **p)
     if (rc) return rc;
     if (bytes == 0) bytes = 16;
     cudaError_t e = cudaMallocFromPoolAsync(p, bytes, g_pool, s ? s : g_stream);
+    if (e == cudaErrorMemoryAllocation) {
+        // Freed blocks stay cached in the pool (no trim between steps).  When the cached blocks of
+        // many different sizes leave none that fits, let the frees queued so far run, give the
+        // unused cache back to the driver and try once more.
+        cudaGetLastError();
+        cudaDeviceSynchronize();
+        cudaMemPoolTrimTo(g_pool, 0);
+        g_trims.fetch_add(1, std::memory_order_relaxed);
+        e = cudaMallocFromPoolAsync(p, bytes, g_pool, s ? s : g_stream);
+    }
     if (e != cudaSuccess) {
         cudaGetLastError();
         return set_error(PTK_ERR_NOMEM, "device allocation of %zu bytes failed: %s", bytes,
@@ -357,5 +368,7 @@ int ptk_pool_stats(size_t *reserved, size_t *used)
 }
 
 long long ptk_launch_count(void) { return launches_issued(); }
+
+long long ptk_pool_trim_count(void) { return ptk::g_trims.load(std::memory_order_relaxed); }
 
 }  // extern "C"
