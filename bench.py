@@ -488,6 +488,7 @@ def run_served(args, kind, world, rank, local):
         "peak_active": best["peak_active"], "peak_bytes": best["peak_bytes"],
         "wall_breakdown_s": {k: best[k] for k in ("wall_s", "chunk_device_s", "admit_s", "retire_s", "schedule_s")},
         "chunks": best["chunks"], "graph_captures": best["graph_captures"], "pool_trims": best["pool_trims"],
+        "admit_waits": best["admit_waits"],
         "plain": {"solves_per_s": len(reqs) / plain["wall_s"], "mcell_updates_per_s": cells / plain["wall_s"] / 1e6,
                   "p50_latency_s": plain["p50_latency_s"], "p99_latency_s": plain["p99_latency_s"],
                   "wall_s": plain["wall_s"]},

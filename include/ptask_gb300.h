@@ -290,6 +290,7 @@ typedef struct ptk_server_stats {
      * maps), retiring them (checksums, result copies) and scheduling (work list, graph capture) */
     double chunk_device_s, admit_s, retire_s, schedule_s;
     long long graph_captures;
+    long long admit_waits;         /* admissions put off because the pool had no block that fit */
 } ptk_server_stats;
 
 int ptk_server_create(const ptk_server_config *cfg, ptk_server **out);

@@ -54,7 +54,8 @@ class ServerStats(C.Structure):
                 ("mean_latency_s", C.c_double), ("cell_updates", C.c_double), ("mcells_per_s", C.c_double),
                 ("chunks", C.c_longlong), ("kernel_launches", C.c_longlong), ("peak_active", C.c_int),
                 ("peak_bytes", C.c_size_t), ("chunk_device_s", C.c_double), ("admit_s", C.c_double),
-                ("retire_s", C.c_double), ("schedule_s", C.c_double), ("graph_captures", C.c_longlong)]
+                ("retire_s", C.c_double), ("schedule_s", C.c_double), ("graph_captures", C.c_longlong),
+                ("admit_waits", C.c_longlong)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}

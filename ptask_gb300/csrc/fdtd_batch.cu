@@ -137,13 +137,39 @@ struct Inst {
     double checksum[6] = {};
     std::vector<float> result[6];
     bool finished = false;
+    void *block = nullptr;      // the one device allocation holding all of the above arrays
 };
 
-size_t instance_bytes(const Layout &L, int nwave)
+// An instance's arrays live in one device allocation (few, large blocks keep the pool's free space
+// usable when thousands of requests of different sizes come and go): byte offsets, each array
+// 256-byte aligned.
+struct InstBlock {
+    size_t field[2][6], coef[4], mat, sum, tma, tab, wave, total;
+};
+
+InstBlock block_layout(const Layout &L, int nwave)
 {
-    return (size_t)L.total * (sizeof(float) * 16 + 1) + (size_t)nwave * sizeof(float) + 6 * sizeof(double) +
-           kTmaSetBytes + (size_t)kMaxMaterials * 4 * sizeof(float) + 4096;
+    InstBlock b{};
+    size_t o = 0;
+    auto take = [&o](size_t bytes) {
+        const size_t at = o;
+        o += (bytes + 255) / 256 * 256;
+        return at;
+    };
+    const size_t a = (size_t)L.total * sizeof(float);
+    for (int p = 0; p < 2; ++p)
+        for (int f = 0; f < 6; ++f) b.field[p][f] = take(a);
+    for (int c = 0; c < 4; ++c) b.coef[c] = take(a);
+    b.mat = take((size_t)L.total);
+    b.sum = take(6 * sizeof(double));
+    b.tma = take(kTmaSetBytes);
+    b.tab = take((size_t)kMaxMaterials * 4 * sizeof(float));
+    b.wave = take((size_t)std::max(nwave, 1) * sizeof(float));
+    b.total = o;
+    return b;
 }
+
+size_t instance_bytes(const Layout &L, int nwave) { return block_layout(L, nwave).total; }
 
 }  // namespace ptk
 
@@ -187,8 +213,9 @@ struct ptk_server {
         std::vector<Inst *> gone;   // instances that finish with this chunk (retired behind it)
     } flight[2];
     bool dirty = true;
+    bool admit_blocked = false;     // the pool could not place a request: wait for retirements
     std::map<std::tuple<int, int, int, int, long long>, cudaGraphExec_t> graphs;
-    long long chunks = 0, launches = 0, captures = 0;
+    long long chunks = 0, launches = 0, captures = 0, admit_waits = 0;
     double wall_s = 0, cell_updates = 0;
     double chunk_dev_s = 0, admit_s = 0, retire_s = 0, sched_s = 0;   // where wall_s went
     cudaEvent_t ev_start[2] = {}, ev_end[2] = {};   // around each chunk replay, per slot
@@ -336,16 +363,22 @@ int admit(ptk_server *s, Inst *in)
     in->steps_total = in->desc.steps;
     const size_t bytes = (size_t)in->L.total * sizeof(float);
     cudaStream_t st = s->st;
-    for (int b = 0; b < 2 && !rc; ++b)
-        for (int f = 0; f < 6 && !rc; ++f) rc = pool_alloc(bytes, st, (void **)&in->buf[b][f]);
-    for (int c = 0; c < 4 && !rc; ++c) rc = pool_alloc(bytes, st, (void **)&in->coef[c]);
-    if (!rc) rc = pool_alloc(6 * sizeof(double), st, (void **)&in->d_sum);
-    if (!rc && s->stages) rc = pool_alloc(kTmaSetBytes, st, &in->tma);
-    if (!rc && s->stages) rc = pool_alloc((size_t)in->L.total, st, (void **)&in->mat);
-    if (!rc && s->stages) rc = pool_alloc((size_t)kMaxMaterials * 4 * sizeof(float), st, (void **)&in->mat_tab);
     in->nwave = (si >= 0 && !wave.empty()) ? (int)wave.size() : 0;
-    if (!rc && in->nwave) rc = pool_alloc(wave.size() * sizeof(float), st, (void **)&in->wave);
+    // One allocation, the first device operation: if it fails nothing needs undoing.
+    const InstBlock lay = block_layout(in->L, in->nwave);
+    rc = pool_alloc(lay.total, st, &in->block);
     if (rc) return rc;
+    char *base = static_cast<char *>(in->block);
+    for (int b = 0; b < 2; ++b)
+        for (int f = 0; f < 6; ++f) in->buf[b][f] = reinterpret_cast<float *>(base + lay.field[b][f]);
+    for (int c = 0; c < 4; ++c) in->coef[c] = reinterpret_cast<float *>(base + lay.coef[c]);
+    in->d_sum = reinterpret_cast<double *>(base + lay.sum);
+    if (s->stages) {
+        in->tma = base + lay.tma;
+        in->mat = reinterpret_cast<unsigned char *>(base + lay.mat);
+        in->mat_tab = reinterpret_cast<float *>(base + lay.tab);
+    }
+    if (in->nwave) in->wave = reinterpret_cast<float *>(base + lay.wave);
     for (int b = 0; b < 2; ++b)
         for (int f = 0; f < 6; ++f) PTK_CUDA_TRY(cudaMemsetAsync(in->buf[b][f], 0, bytes, st));
     if (in->mat) PTK_CUDA_TRY(cudaMemsetAsync(in->mat, 0, (size_t)in->L.total, st));
@@ -394,19 +427,16 @@ int admit(ptk_server *s, Inst *in)
 
 void release(ptk_server *s, Inst *in)
 {
-    for (int b = 0; b < 2; ++b)
-        for (int f = 0; f < 6; ++f) pool_free(in->buf[b][f], s->st);
-    for (int c = 0; c < 4; ++c) pool_free(in->coef[c], s->st);
-    pool_free(in->wave, s->st);
-    pool_free(in->d_sum, s->st);
-    pool_free(in->tma, s->st);
-    in->tma = nullptr;
-    pool_free(in->mat, s->st);
-    pool_free(in->mat_tab, s->st);
-    in->mat = nullptr;
-    in->mat_tab = nullptr;
+    pool_free(in->block, s->st);
+    in->block = nullptr;
     for (int b = 0; b < 2; ++b)
         for (int f = 0; f < 6; ++f) in->buf[b][f] = nullptr;
+    for (int c = 0; c < 4; ++c) in->coef[c] = nullptr;
+    in->wave = nullptr;
+    in->d_sum = nullptr;
+    in->tma = nullptr;
+    in->mat = nullptr;
+    in->mat_tab = nullptr;
     s->used -= in->bytes;
 }
 
@@ -692,7 +722,8 @@ int ptk_server_run(ptk_server *s, double time_scale)
         double t = clock();
         s->up_used[s->par] = 0;   // this half's copies preceded a chunk that has landed
         // admit arrived requests, FIFO, while they fit the budget and the slot limit
-        while (nxt < order.size() && arrived(order[nxt], t) && (int)s->active.size() < s->cfg.max_active) {
+        while (nxt < order.size() && !s->admit_blocked && arrived(order[nxt], t) &&
+               (int)s->active.size() < s->cfg.max_active) {
             Inst *in = order[nxt];
             const size_t need = instance_bytes(make_layout(in->desc.Nx, in->desc.Ny, in->desc.Nz), in->desc.steps);
             if (s->used + need > s->cfg.hbm_budget_bytes) break;
@@ -700,6 +731,16 @@ int ptk_server_run(ptk_server *s, double time_scale)
             const double ta = now_s();
             rc = admit(s, in);
             s->admit_s += now_s() - ta;
+            if (rc == PTK_ERR_NOMEM && (!s->active.empty() || s->flight[0].on || s->flight[1].on)) {
+                // Within the budget but the pool has no block that fits right now: back-pressure,
+                // not a failure.  Try again once running requests have retired and freed theirs.
+                clear_error();
+                rc = PTK_OK;
+                in->t_admit = -1;
+                s->admit_blocked = true;
+                ++s->admit_waits;
+                break;
+            }
             if (rc) break;
             ++nxt;
         }
@@ -714,6 +755,10 @@ int ptk_server_run(ptk_server *s, double time_scale)
                 break;
             }
             s->up_used[0] = s->up_used[1] = 0;
+            if (s->admit_blocked) {   // everything has retired and its memory is free: try again
+                s->admit_blocked = false;
+                continue;
+            }
             if (nxt < order.size()) {
                 const double wait = order[nxt]->t_arrival * time_scale - clock();
                 if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.01)));
@@ -775,6 +820,7 @@ int ptk_server_run(ptk_server *s, double time_scale)
             }
             if (rc) break;
             s->dirty = true;
+            s->admit_blocked = false;   // memory was freed: admission may try again
         }
         if (cudaEventRecord(s->ev_ret[b], s->st) != cudaSuccess) {
             rc = set_error(PTK_ERR_CUDA, "event record failed");
@@ -856,6 +902,7 @@ int ptk_server_stats_get(ptk_server *s, ptk_server_stats *st)
     st->retire_s = s->retire_s;
     st->schedule_s = s->sched_s;
     st->graph_captures = s->captures;
+    st->admit_waits = s->admit_waits;
     return PTK_OK;
 }
 

@@ -92,8 +92,11 @@ int pool_alloc(size_t bytes, cudaStream_t s, void **p)
     int rc = ensure_init();
     if (rc) return rc;
     if (bytes == 0) bytes = 16;
-    cudaError_t e = cudaMallocFromPoolAsync(p, bytes, g_pool, s ? s : g_stream);
-    if (e == cudaErrorMemoryAllocation) {
+    cudaStream_t st = s ? s : g_stream;
+    cudaError_t e = cudaMallocFromPoolAsync(p, bytes, g_pool, st);
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (e == cudaErrorMemoryAllocation && cudaStreamIsCapturing(st, &cs) == cudaSuccess &&
+        cs == cudaStreamCaptureStatusNone) {
         // Freed blocks stay cached in the pool (no trim between steps).  When the cached blocks of
         // many different sizes leave none that fits, let the frees queued so far run, give the
         // unused cache back to the driver and try once more.
@@ -101,7 +104,7 @@ int pool_alloc(size_t bytes, cudaStream_t s, void **p)
         cudaDeviceSynchronize();
         cudaMemPoolTrimTo(g_pool, 0);
         g_trims.fetch_add(1, std::memory_order_relaxed);
-        e = cudaMallocFromPoolAsync(p, bytes, g_pool, s ? s : g_stream);
+        e = cudaMallocFromPoolAsync(p, bytes, g_pool, st);
     }
     if (e != cudaSuccess) {
         cudaGetLastError();
