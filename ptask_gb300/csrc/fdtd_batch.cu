@@ -211,6 +211,7 @@ struct ptk_server {
     struct Flight {
         bool on = false;
         std::vector<Inst *> gone;   // instances that finish with this chunk (retired behind it)
+        cudaGraphExec_t exec = nullptr;   // the chunk graph it replays
     } flight[2];
     bool dirty = true;
     bool admit_blocked = false;     // the pool could not place a request: wait for retirements
@@ -486,6 +487,8 @@ int rebuild_worklist(ptk_server *s)
     return PTK_OK;
 }
 
+constexpr size_t kMaxGraphs = 256;   // chunk graphs kept for reuse
+
 int chunk_graph(ptk_server *s, int len, int grid, cudaGraphExec_t *out)
 {
     const int n = (int)s->active.size();
@@ -523,6 +526,19 @@ int chunk_graph(ptk_server *s, int len, int grid, cudaGraphExec_t *out)
     e = cudaGraphInstantiate(&ex, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return set_error(PTK_ERR_CUDA, "chunk instantiate: %s", cudaGetErrorString(e));
+    // Bounded cache: under a changing request mix most work lists never repeat.  Evict all but the
+    // graph of the chunk that may still be queued or running (slot par ^ 1; slot par has landed).
+    if (s->graphs.size() >= kMaxGraphs) {
+        const cudaGraphExec_t busy = s->flight[s->par ^ 1].on ? s->flight[s->par ^ 1].exec : nullptr;
+        for (auto it = s->graphs.begin(); it != s->graphs.end();) {
+            if (it->second == busy) {
+                ++it;
+            } else {
+                cudaGraphExecDestroy(it->second);
+                it = s->graphs.erase(it);
+            }
+        }
+    }
     s->graphs[key] = ex;
     ++s->captures;
     *out = ex;
@@ -783,6 +799,7 @@ int ptk_server_run(ptk_server *s, double time_scale)
             rc = set_error(PTK_ERR_CUDA, "chunk launch failed");
             break;
         }
+        s->flight[b].exec = ex;
         // kernels in the chunk graph: the steps, the step-counter advance and (staged) the faces
         const int kernels = len + 1 + (s->stages && s->total_faces > 0 ? 1 : 0);
         count_graph_launch(kernels);
