@@ -122,3 +122,21 @@ def test_batched_config_generator_shapes():
     assert e.min() >= 32 and e.max() <= 192
     assert all(100 <= r.steps <= 2000 for r in reqs)
     assert all(1 <= r.n_boxes <= 8 for r in reqs)
+
+
+def test_many_work_lists_evict_cached_graphs_and_stay_exact():
+    """Hundreds of small requests finishing at staggered steps give hundreds of different work lists;
+    the server keeps at most 256 chunk graphs (evicting all but the one a queued chunk replays) and
+    every result still equals the solo solve."""
+    # every request finishes at a step of its own: 320 chunk boundaries, each a new work list
+    reqs = [Request(8 + q % 7, 8 + (q * 3) % 5, 6 + q % 4, 3 + q, 1, 1000 + q) for q in range(320)]
+    with Server(keep_results=True, chunk_steps=4) as s:
+        tickets = [s.submit(r) for r in reqs]
+        s.run(time_scale=0)
+        st = s.stats()
+        assert st["completed"] == len(reqs) and st["graph_captures"] > 256
+        for q in range(0, len(reqs), 29):
+            got = s.fetch(tickets[q])
+            ref, _ = alone(reqs[q])
+            for f in range(6):
+                np.testing.assert_array_equal(got[f], ref[f], err_msg=f"request {q} field {P.FIELDS[f]}")
