@@ -431,3 +431,31 @@ def test_pinned_host_buffers_are_reused_by_size():
     assert c.value != b.value
     for p in (b, c):
         assert lib.ptk_host_free(p) == 0
+
+
+# ------------------------------------------------------------------------------------------------
+# Randomised parity: seeded shapes x every staged tile shape x depths x material index on / off.
+# ------------------------------------------------------------------------------------------------
+STAGED_SHAPES = [(4, 3), (8, 4), (10, 4), (11, 4), (11, 3), (7, 4), (23, 4), (23, 3), (8, 6), (4, 5)]
+
+
+@pytest.mark.parametrize("case", range(24))
+def test_staged_kernel_random_shapes(case):
+    rng = np.random.default_rng(9000 + case)
+    shape = tuple(int(v) for v in rng.integers(1, 72, size=3))
+    by, stages = STAGED_SHAPES[case % len(STAGED_SHAPES)]
+    kc = int(rng.choice([0, 1, 2, 5, 17]))
+    steps = int(rng.integers(2, 8))
+    use_mat = bool(case % 3)
+    n_boxes = int(rng.integers(1, 4)) if min(shape) >= 4 else 0
+    pr = P.Problem.generate(*shape, n_boxes=n_boxes, eps=(1, 9), box=(2, max(2, min(shape) // 2)), steps=steps,
+                            source_mode=1 if min(shape) >= 3 else 0, seed=700 + case)
+    f = P.random_fields(*shape, seed=800 + case, scale=1e-2)
+    ref = oracle.step_ext_f32(f, steps, pr.params, pr.Ca, pr.Cb, pr.Da, pr.Db, pr.src, pr.wave)
+    with P.Solver(pr.params) as s:
+        s.set_tiles(by, kc, 4, stages)
+        s.set_problem(pr)
+        s.use_material_index(use_mat)
+        s.set_fields(f)
+        s.run(steps)
+        assert_parity(s.get_fields(), ref, f"{shape} by={by} stages={stages} kc={kc} mat={use_mat}")
