@@ -600,7 +600,7 @@ void retire_finish(ptk_server *s, Inst *in, const double *h_slot, double t)
 extern "C" {
 
 int ptk_server_create(const ptk_server_config *cfg, ptk_server **out)
-{
+try {
     clear_error();
     PTK_CHECK_ARG(cfg && out, "NULL argument");
     int rc = ensure_init();
@@ -670,10 +670,10 @@ int ptk_server_create(const ptk_server_config *cfg, ptk_server **out)
     }
     *out = s;
     return PTK_OK;
-}
+} PTK_CATCH_ALL
 
 int ptk_server_submit(ptk_server *s, const ptk_problem_desc *d, double arrival_s, long long *ticket)
-{
+try {
     PTK_CHECK_ARG(s && d, "NULL argument");
     PTK_CHECK_ARG(d->Nx >= 1 && d->Ny >= 1 && d->Nz >= 1 && d->steps >= 1, "bad request %dx%dx%d x %d steps",
                   d->Nx, d->Ny, d->Nz, d->steps);
@@ -691,10 +691,10 @@ int ptk_server_submit(ptk_server *s, const ptk_problem_desc *d, double arrival_s
     s->all.push_back(in);
     if (ticket) *ticket = in->ticket;
     return PTK_OK;
-}
+} PTK_CATCH_ALL
 
 int ptk_server_run(ptk_server *s, double time_scale)
-{
+try {
     clear_error();
     PTK_CHECK_ARG(s, "NULL server");
     std::lock_guard<std::mutex> lk(s->mu);
@@ -855,7 +855,7 @@ int ptk_server_run(ptk_server *s, double time_scale)
     if (rc != PTK_OK) cudaStreamSynchronize(s->st);
     s->wall_s += clock();
     return rc;
-}
+} PTK_CATCH_ALL
 
 int ptk_server_request(ptk_server *s, long long ticket, ptk_request_info *info)
 {
@@ -876,7 +876,7 @@ int ptk_server_request(ptk_server *s, long long ticket, ptk_request_info *info)
 }
 
 int ptk_server_fetch(ptk_server *s, long long ticket, float *const fields[6])
-{
+try {
     PTK_CHECK_ARG(s && fields, "NULL argument");
     if (ticket < 0 || ticket >= (long long)s->all.size()) return set_error(PTK_ERR_NOTFOUND, "no ticket %lld", ticket);
     Inst *in = s->all[(size_t)ticket];
@@ -884,10 +884,10 @@ int ptk_server_fetch(ptk_server *s, long long ticket, float *const fields[6])
     if (in->result[0].empty()) return set_error(PTK_ERR_STATE, "server was created without keep_results");
     for (int f = 0; f < 6; ++f) memcpy(fields[f], in->result[f].data(), in->result[f].size() * sizeof(float));
     return PTK_OK;
-}
+} PTK_CATCH_ALL
 
 int ptk_server_stats_get(ptk_server *s, ptk_server_stats *st)
-{
+try {
     PTK_CHECK_ARG(s && st, "NULL argument");
     std::vector<double> lat;
     for (Inst *in : s->all)
@@ -921,7 +921,7 @@ int ptk_server_stats_get(ptk_server *s, ptk_server_stats *st)
     st->graph_captures = s->captures;
     st->admit_waits = s->admit_waits;
     return PTK_OK;
-}
+} PTK_CATCH_ALL
 
 int ptk_server_destroy(ptk_server *s)
 {

@@ -286,7 +286,7 @@ static int validate_params(const ptk_fdtd_params *p)
 extern "C" {
 
 int ptk_solver_create(const ptk_fdtd_params *p, ptk_solver **out)
-{
+try {
     clear_error();
     int rc = validate_params(p);
     if (rc) return rc;
@@ -338,7 +338,7 @@ int ptk_solver_create(const ptk_fdtd_params *p, ptk_solver **out)
     }
     *out = s;
     return PTK_OK;
-}
+} PTK_CATCH_ALL
 
 int ptk_solver_destroy(ptk_solver *s)
 {
@@ -572,12 +572,12 @@ int ptk_solver_get_tiles(const ptk_solver *s, ptk_tile_config *cfg)
 }
 
 int ptk_solver_run(ptk_solver *s, int steps, void *stream)
-{
+try {
     clear_error();
     PTK_CHECK_ARG(s, "NULL solver");
     std::lock_guard<std::mutex> lk(s->mu);
     return solver_run(s, steps, S(stream));
-}
+} PTK_CATCH_ALL
 
 int ptk_solver_bytes(const ptk_solver *s, size_t *bytes)
 {
@@ -596,7 +596,7 @@ int ptk_solver_last_launches(const ptk_solver *s, long long *launches)
 int ptk_fdtd_solve(const ptk_fdtd_params *p, float *const fields[6], const float *Ca, const float *Cb,
                    const float *Da, const float *Db, int si, int sj, int sk, const float *wave,
                    int nwave, int steps, float *ms)
-{
+try {
     clear_error();
     ptk_solver *s = nullptr;
     int rc = ptk_solver_create(p, &s);
@@ -618,7 +618,7 @@ int ptk_fdtd_solve(const ptk_fdtd_params *p, float *const fields[6], const float
     cudaEventDestroy(e1);
     ptk_solver_destroy(s);
     return rc;
-}
+} PTK_CATCH_ALL
 
 int ptk_launch_field_update(int field, const float *in0, const float *in1, const float *in2,
                             const ptk_fdtd_params *p, float *out, void *stream)
@@ -664,7 +664,7 @@ static std::mutex g_tune_mu;
 static std::map<std::tuple<int, int, int>, std::pair<ptk_tile_config, float>> g_tune_cache;
 
 int ptk_autotune_tiles(int Nx, int Ny, int Nz, ptk_tile_config *best, float *best_ms)
-{
+try {
     clear_error();
     PTK_CHECK_ARG(best, "NULL argument");
     {
@@ -770,6 +770,6 @@ int ptk_autotune_tiles(int Nx, int Ny, int Nz, ptk_tile_config *best, float *bes
     *best = bc;
     if (best_ms) *best_ms = best_t;
     return PTK_OK;
-}
+} PTK_CATCH_ALL
 
 }  // extern "C"

@@ -16,6 +16,14 @@
 
 #include "ptk_problem.h"
 
+#include <exception>
+#include <new>
+
+// No C++ exception unwinds into a C caller of the entry point below.
+#define PTK_PROBLEM_CATCH_ALL                              \
+    catch (const std::bad_alloc &) { return PTK_ERR_NOMEM; } \
+    catch (...) { return PTK_ERR_STATE; }
+
 namespace {
 
 struct Rng {
@@ -132,7 +140,7 @@ int ptk_fill_uniform(float *dst, size_t n, float scale, uint64_t seed)
 
 int ptk_problem_generate(const ptk_problem_desc *d, ptk_fdtd_params *p, float *Ca, float *Cb, float *Da,
                          float *Db, int *si, int *sj, int *sk, float *wave)
-{
+try {
     std::vector<ptk::BoxSpec> boxes;
     std::vector<float> w;
     int rc = ptk::problem_plan(d, p, &boxes, si, sj, sk, &w);
@@ -154,6 +162,6 @@ int ptk_problem_generate(const ptk_problem_desc *d, ptk_fdtd_params *p, float *C
     if (wave)
         for (size_t n = 0; n < w.size(); ++n) wave[n] = w[n];
     return PTK_OK;
-}
+} PTK_PROBLEM_CATCH_ALL
 
 }  // extern "C"

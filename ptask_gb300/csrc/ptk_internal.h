@@ -5,6 +5,8 @@
 #include <algorithm>
 #include <cstddef>
 #include <cstdint>
+#include <exception>
+#include <new>
 #include <string>
 #include <utility>
 #include <vector>
@@ -18,6 +20,13 @@ namespace ptk {
 // thread-local message for ptk_last_error() and returns the code.
 // ---------------------------------------------------------------------------------------------
 int set_error(int code, const char *fmt, ...);
+
+// Handlers of the C entry points' function-try-blocks: no C++ exception (a host allocation that
+// throws std::bad_alloc, say) unwinds into a C caller; it becomes a status and ptk_last_error().
+#define PTK_CATCH_ALL                                                                                  \
+    catch (const std::bad_alloc &) { return ptk::set_error(PTK_ERR_NOMEM, "host allocation failed"); } \
+    catch (const std::exception &e) { return ptk::set_error(PTK_ERR_STATE, "unexpected error: %s", e.what()); } \
+    catch (...) { return ptk::set_error(PTK_ERR_STATE, "unexpected error"); }
 void clear_error();
 
 #define PTK_CUDA_TRY(expr)                                                                        \

@@ -294,10 +294,15 @@ int bind_loaded(ptk_fdtd_graph *G, int mode)
 
 }  // namespace
 
+// No C++ exception unwinds into a C caller of the entry points below.
+#define PTK_GRAPH_CATCH_ALL                                \
+    catch (const std::bad_alloc &) { return PTK_ERR_NOMEM; } \
+    catch (...) { return PTK_ERR_STATE; }
+
 extern "C" {
 
 int ptk_fdtd_graph_create(const ptk_fdtd_params *p, int mode, int unrolled_steps, ptk_fdtd_graph **out)
-{
+try {
     if (!p || !out || p->Nx < 1 || p->Ny < 1 || p->Nz < 1 || mode < 0 || mode > 3) return PTK_ERR_INVALID;
     if (mode == PTK_GRAPH_UNROLLED && unrolled_steps < 1) return PTK_ERR_INVALID;
     Runtime::SetExitOnRuntimeFailure(FALSE);
@@ -308,11 +313,11 @@ int ptk_fdtd_graph_create(const ptk_fdtd_params *p, int mode, int unrolled_steps
     start(G);
     *out = G;
     return PTK_OK;
-}
+} PTK_GRAPH_CATCH_ALL
 
 int ptk_fdtd_graph_create_host(const ptk_fdtd_params *p, int unrolled_steps, const char *library,
                                unsigned host_fields, ptk_fdtd_graph **out)
-{
+try {
     if (!p || !out || !library || p->Nx < 1 || p->Ny < 1 || p->Nz < 1 || unrolled_steps < 1 || host_fields > 0x3Fu)
         return PTK_ERR_INVALID;
     Runtime::SetExitOnRuntimeFailure(FALSE);
@@ -328,10 +333,10 @@ int ptk_fdtd_graph_create_host(const ptk_fdtd_params *p, int unrolled_steps, con
     start(G);
     *out = G;
     return PTK_OK;
-}
+} PTK_GRAPH_CATCH_ALL
 
 int ptk_fdtd_graph_export(const ptk_fdtd_params *p, int mode, int unrolled_steps, const char *path)
-{
+try {
     if (!p || !path || p->Nx < 1 || p->Ny < 1 || p->Nz < 1 || mode < 0 || mode > 3) return PTK_ERR_INVALID;
     if (mode == PTK_GRAPH_UNROLLED && unrolled_steps < 1) return PTK_ERR_INVALID;
     Runtime::SetExitOnRuntimeFailure(FALSE);
@@ -343,17 +348,17 @@ int ptk_fdtd_graph_export(const ptk_fdtd_params *p, int mode, int unrolled_steps
     Graph::DestroyGraph(G->g);
     delete G;
     return rc;
-}
+} PTK_GRAPH_CATCH_ALL
 
 int ptk_fdtd_graph_save(ptk_fdtd_graph *G, const char *path)
-{
+try {
     if (!G || !path) return PTK_ERR_INVALID;
     G->g->Serialize(path);
     return *G->g->GetSerializationError() ? PTK_ERR_STATE : PTK_OK;
-}
+} PTK_GRAPH_CATCH_ALL
 
 int ptk_fdtd_graph_load(const ptk_fdtd_params *p, int mode, const char *path, ptk_fdtd_graph **out)
-{
+try {
     if (!p || !path || !out || p->Nx < 1 || p->Ny < 1 || p->Nz < 1 || mode < 0 || mode > 3) return PTK_ERR_INVALID;
     Runtime::SetExitOnRuntimeFailure(FALSE);
     if (PTFAILED(Runtime::Initialize())) return PTK_ERR_CUDA;
@@ -368,10 +373,10 @@ int ptk_fdtd_graph_load(const ptk_fdtd_params *p, int mode, const char *path, pt
     start(G);
     *out = G;
     return PTK_OK;
-}
+} PTK_GRAPH_CATCH_ALL
 
 int ptk_graph_xml_roundtrip(const char *in_path, const char *out_path)
-{
+try {
     if (!in_path || !out_path) return PTK_ERR_INVALID;
     Runtime::SetExitOnRuntimeFailure(FALSE);
     Graph *g = new Graph("roundtrip");
@@ -383,11 +388,11 @@ int ptk_graph_xml_roundtrip(const char *in_path, const char *out_path)
     }
     Graph::DestroyGraph(g);
     return rc;
-}
+} PTK_GRAPH_CATCH_ALL
 
 int ptk_fdtd_graph_set_problem(ptk_fdtd_graph *G, const float *Ca, const float *Cb, const float *Da, const float *Db,
                                int si, int sj, int sk, const float *wave, int nwave)
-{
+try {
     if (!G) return PTK_ERR_INVALID;
     if (G->mode == PTK_GRAPH_UNROLLED) {
         // The reference's tasks use the scalar coefficients of FDTD_PARAMS and have no source.
@@ -423,7 +428,7 @@ int ptk_fdtd_graph_set_problem(ptk_fdtd_graph *G, const float *Ca, const float *
     if (rc) return rc;
     G->problem_set = true;
     return PTK_OK;
-}
+} PTK_GRAPH_CATCH_ALL
 
 static int solve_impl(ptk_fdtd_graph *G, float *const fields[6], int instances, float *const results[], int steps)
 {
@@ -464,16 +469,16 @@ static int solve_impl(ptk_fdtd_graph *G, float *const fields[6], int instances, 
 }
 
 int ptk_fdtd_graph_solve(ptk_fdtd_graph *G, float *const fields[6], int steps)
-{
+try {
     return solve_impl(G, fields, 1, nullptr, steps);
-}
+} PTK_GRAPH_CATCH_ALL
 
 int ptk_fdtd_graph_solve_many(ptk_fdtd_graph *G, float *const fields[6], int instances, float *const results[],
                               int steps)
-{
+try {
     if (!results) return PTK_ERR_INVALID;
     return solve_impl(G, fields, instances, results, steps);
-}
+} PTK_GRAPH_CATCH_ALL
 
 int ptk_fdtd_graph_stats(const ptk_fdtd_graph *G, ptk_graph_stats *st)
 {
