@@ -298,7 +298,10 @@ int ptk_server_create(const ptk_server_config *cfg, ptk_server **out);
  * arrival_s on the trace clock.  Rejects requests larger than the whole budget. */
 int ptk_server_submit(ptk_server *s, const struct ptk_problem_desc *d, double arrival_s, long long *ticket);
 /* Serve every queued request.  Arrival times are multiplied by time_scale (0: all available at
- * once); requests are admitted in arrival order as they arrive and fit. */
+ * once); requests are admitted in arrival order as they arrive and fit the HBM budget.  A request
+ * that fits the budget but finds no free device block waits for running requests to retire.
+ * submit, run, request, fetch and stats_get are serialised by the server's lock: called from
+ * another thread during a run, they wait for it to finish. */
 int ptk_server_run(ptk_server *s, double time_scale);
 int ptk_server_request(ptk_server *s, long long ticket, ptk_request_info *info);
 /* Host copy of a finished request's fields (reference layout); needs keep_results. */

@@ -860,6 +860,7 @@ try {
 int ptk_server_request(ptk_server *s, long long ticket, ptk_request_info *info)
 {
     PTK_CHECK_ARG(s && info, "NULL argument");
+    std::lock_guard<std::mutex> lk(s->mu);   // waits for a run in progress
     if (ticket < 0 || ticket >= (long long)s->all.size()) return set_error(PTK_ERR_NOTFOUND, "no ticket %lld", ticket);
     Inst *in = s->all[(size_t)ticket];
     info->ticket = ticket;
@@ -878,6 +879,7 @@ int ptk_server_request(ptk_server *s, long long ticket, ptk_request_info *info)
 int ptk_server_fetch(ptk_server *s, long long ticket, float *const fields[6])
 try {
     PTK_CHECK_ARG(s && fields, "NULL argument");
+    std::lock_guard<std::mutex> lk(s->mu);
     if (ticket < 0 || ticket >= (long long)s->all.size()) return set_error(PTK_ERR_NOTFOUND, "no ticket %lld", ticket);
     Inst *in = s->all[(size_t)ticket];
     if (!in->finished) return set_error(PTK_ERR_STATE, "request %lld has not finished", ticket);
@@ -889,6 +891,7 @@ try {
 int ptk_server_stats_get(ptk_server *s, ptk_server_stats *st)
 try {
     PTK_CHECK_ARG(s && st, "NULL argument");
+    std::lock_guard<std::mutex> lk(s->mu);
     std::vector<double> lat;
     for (Inst *in : s->all)
         if (in->finished) lat.push_back(in->t_finish - in->t_arrival_run);
