@@ -66,8 +66,10 @@ class Server:
 
     def __init__(self, budget_bytes: int = 0, max_active: int = 0, chunk_steps: int = 32, tile_rows: int = 0,
                  keep_results: bool = False, persistent: bool = True, stages: int = 0):
-        """`stages`: 0 = TMA-staged step kernel with its default ring, 2..5 = that many planes,
-        -1 = register kernel."""
+        """`tile_rows`: 0 = 11 (128-wide tiles); 7 and 23 give 64-wide tiles (7 rows: four-warp CTAs,
+        three per SM), which suit mixes of narrow requests.  `stages`: 0 = TMA-staged step kernel
+        with its default ring, 2..6 = that many planes where the rows have that shape, -1 = register
+        kernel.  `budget_bytes` 0 = 80 % of the free device memory at creation."""
         lib()
         self._h = C.c_void_p()
         self.cfg = ServerConfig(budget_bytes, max_active, chunk_steps, tile_rows, int(keep_results), int(persistent),
