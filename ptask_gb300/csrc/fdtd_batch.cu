@@ -1,13 +1,21 @@
 // fdtd_batch.cu -- batched and served FDTD: many device-resident instances of uneven size advanced
 // together by the fused step kernel, with continuous admission by HBM budget.
 //
-// One time step of every active instance is ONE launch of k_yee_step over the concatenated tile
-// lists of all instances (a persistent grid of resident CTAs walks the list), and chunks of steps
-// are replayed as captured CUDA graphs.  Instances finish at their own step counts: their tiles go
-// idle inside the chunk in which they finish and they leave the batch at the chunk boundary, where
-// newly arrived requests are admitted if their fields fit the HBM budget.  Request problems are
-// generated on the device (coefficients from the seeded box list), so admission moves only the
-// source waveform over the host link.
+// One time step of every active instance is ONE launch of the step kernel (the TMA-staged
+// k_yee_step_bulk with a material index by default, the register kernel k_yee_step on request) over
+// the concatenated tile lists of all instances: a persistent grid of resident CTAs takes tiles from
+// a counter.  Chunks of steps are replayed as captured CUDA graphs (at most kMaxGraphs kept).
+// Instances finish at their own step counts: their tiles go idle inside the chunk in which they
+// finish and they leave the batch at the chunk boundary, where newly arrived requests are admitted
+// if they fit the HBM budget.  Request problems are generated on the device (coefficients and the
+// material index from the seeded box list), so admission moves only the waveform and the tensor
+// maps over the host link.
+//
+// The host keeps one chunk queued ahead: while chunk i runs it admits, rebuilds the work list into
+// the other half of a double-buffered pinned staging area and launches chunk i+1, with chunk i's
+// finishers retired (fixed-order FP64 checksums, frees) in stream order between them; only then
+// does it wait for chunk i.  Each instance's arrays are one device block; an admission that fits
+// the budget but finds no free block waits for retirements instead of failing.
 //
 // The reference has no batching: it pipelines numBlocks copies of one problem through one graph
 // (graphfdtd.cpp:1076-1097) and dispatches every task of every copy separately.
