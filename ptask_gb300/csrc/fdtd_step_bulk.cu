@@ -1,10 +1,11 @@
 // fdtd_step_bulk.cu -- the fused Yee step with its operands staged by the TMA engine.
 //
-// Same arithmetic, tiles, work list and results as k_yee_step (fdtd_kernels.cu), different data
-// movement.  For every z plane of a 128 x BY tile, the rows of the ten arrays that the plane needs
-// (own rows plus the y-1 / y+1 halo rows, 136 floats wide to cover the x-1 / x+1 halo) arrive in
-// shared memory as one TMA tensor copy per array (cp.async.bulk.tensor.3d, box 136 x rows x 1):
-// ten copies per plane, issued by ten lanes of one warp.  Boxes that hang over the grid's edges are
+// Same arithmetic, work list and results as k_yee_step (fdtd_kernels.cu), different data
+// movement.  For every z plane of a W x BY tile (W = 128: a warp per row; W = 64 for 7 and 23 rows:
+// a warp per two half rows), the rows of the ten arrays that the plane needs (own rows plus the
+// y-1 / y+1 halo rows, W+8 floats wide to cover the x-1 / x+1 halo) arrive in shared memory as one
+// TMA tensor copy per array (cp.async.bulk.tensor.3d, box (W+8) x rows x 1): ten copies per plane,
+// issued by ten lanes of one warp.  Boxes that hang over the grid's edges are
 // filled with zeros by the TMA unit.  Planes are loaded ahead into a ring of S stages, each guarded
 // by an mbarrier whose transaction count is the bytes in flight, so the number of bytes in flight
 // does not depend on registers or occupancy.  Compute reads only shared memory; results leave with
