@@ -10,12 +10,18 @@ Courant 0.5, Gaussian Ez source, 1000 steps).  Prints one JSON line (rank 0):
   value  Mcell-updates/s with the inputs already resident in HBM (device events around the solves)
   e2e    the same metric through the public C-ABI path with pinned host buffers, the H2D upload of the
          inputs and the D2H download of the six result fields inside the timed region
-  roofline  the fused step kernel against measured HBM bandwidth, 64 algorithmic bytes per cell update
+  roofline  the fused step kernel against measured HBM bandwidth: 49 algorithmic bytes per cell update
+         with the material index (six fields read and written, one id byte), 64 with per-cell arrays
   cpu_baseline  the CPU oracle (our FP32 port of the reference's fdtd_cpu, OpenMP over all host cores)
                 timed on a bounded sample of the same workload
+  served the workload's batched/served half: the 64-instance batched set, a Poisson trace at the
+         workload's 200 req/s and one below saturation, each served by continuous batching and by
+         every plain one-at-a-time arm (fused server slot, fused graph dispatch, task-wise graph
+         dispatch) on the same requests: solves/s, Mcell/s, p50/p99 and the fraction of peak
 
 --impl reference times the reference's CPU implementation of the path instead (the oracle port; the
-reference's own build needs its source tree, which is absent where this runs) on the same workload.
+reference's own build needs its source tree, which is absent where this runs) on the same workload,
+loading nothing but the oracle.
 Under torchrun each rank runs an independent replica (the path shards by instance; no collective on
 the data path) and rank 0 reports the whole-job aggregate.
 """
@@ -175,8 +181,7 @@ def traffic_per_cell(kernel: str, mat: bool = False, rows: int = 0):
 def cpu_sample(prob, shape, target_s: float = 10.0):
     """Time the oracle (FP32 port of fdtd_cpu, all host threads) on a bounded sample of the workload."""
     import oracle
-    import ptask_gb300 as P
-    f = P.zero_fields(*shape)
+    f = oracle.zero_fields(*shape)
     oracle.step_ext_f32(f, 1, prob.params, prob.Ca, prob.Cb, prob.Da, prob.Db, prob.src, prob.wave)  # warm
     t0 = time.perf_counter()
     oracle.step_ext_f32(f, 2, prob.params, prob.Ca, prob.Cb, prob.Da, prob.Db, prob.src, prob.wave)
@@ -197,19 +202,28 @@ def cpu_sample(prob, shape, target_s: float = 10.0):
     return {"value": cells * steps * repeats / dt / 1e6, "unit": "Mcell-updates/s", "cores": oracle.threads(),
             "kind": "port",
             "sample": f"{shape[0]}x{shape[1]}x{shape[2]} grid, {what} ({dt:.1f} s), oracle/fdtd_oracle.c FP32 "
-                      f"with OpenMP"}
+                      f"port of fdtd_cpu, OpenMP on {oracle.threads()} host threads"}
+
+
+def workload_config(wl, world: int) -> dict:
+    """The `config` object of a plain workload, identical in both arms' lines."""
+    nx, ny, nz = wl["shape"]
+    return {"workload": wl["desc"], "grid": [nx, ny, nz], "time_steps": wl["steps"],
+            "l2": "working set %.2f GB > 129 MB L2; no flush needed" % (16 * 4 * (nx + 1) * (ny + 1) * (nz + 1) / 1e9),
+            "parallelism": f"replicas x{world}"}
 
 
 def run_reference(args, wl, world, rank, local):
-    """--impl reference: the CPU implementation of the path on the host cores."""
+    """--impl reference: the CPU implementation of the path on the host cores.  Everything it runs is
+    the oracle (oracle/: the FP32 port of fdtd_cpu and its own copy of the seeded problem generator);
+    nothing of the product library is loaded."""
     if rank != 0:
         return 0
     import oracle
-    import ptask_gb300 as P
     shape = wl["shape"]
-    prob = P.Problem.generate(*shape, n_boxes=wl["boxes"], eps=wl["eps"], box=wl["box"], steps=wl["steps"],
-                              source_mode=1, seed=2)
-    f = P.zero_fields(*shape)
+    prob = oracle.problem_generate(*shape, n_boxes=wl["boxes"], eps=wl["eps"], box=wl["box"], steps=wl["steps"],
+                                   source_mode=1, seed=2)
+    f = oracle.zero_fields(*shape)
     t0 = time.perf_counter()
     oracle.step_ext_f32(f, 1, prob.params, prob.Ca, prob.Cb, prob.Da, prob.Db, prob.src, prob.wave)
     one = time.perf_counter() - t0
@@ -222,14 +236,16 @@ def run_reference(args, wl, world, rank, local):
     dt = time.perf_counter() - t0
     cells = shape[0] * shape[1] * shape[2]
     value = cells * per * args.steps / dt / 1e6
+    threads = oracle.threads()
     sample = (f"{shape[0]}x{shape[1]}x{shape[2]} grid, {per} of the workload's {wl['steps']} time steps per "
-              f"bench step, oracle/fdtd_oracle.c FP32 port of fdtd_cpu with OpenMP")
+              f"bench step, oracle/fdtd_oracle.c FP32 port of fdtd_cpu, OpenMP on {threads} host threads")
     line = {"metric": "FDTD Mcell-updates/s", "value": value, "unit": "Mcell-updates/s", "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": wl["desc"], "grid": list(shape), "time_steps": wl["steps"]},
-            "cpu_baseline": {"value": value, "unit": "Mcell-updates/s", "cores": oracle.threads(), "kind": "port",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded problem generator)",
+            "config": workload_config(wl, world),
+            "bench_step": f"{per} time steps of the workload on the host cores",
+            "cpu_baseline": {"value": value, "unit": "Mcell-updates/s", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "Mcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -397,15 +413,13 @@ def run_ours(args, wl, world, rank, local):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded problem generator)",
-        "config": {"workload": wl["desc"], "grid": list(shape), "time_steps": T,
-                   "bench_step": "one complete solve (all time steps) from resident initial fields",
-                   "l2": "working set %.2f GB > 129 MB L2; no flush needed" % (16 * 4 * (nx + 1) * (ny + 1) * (nz + 1) / 1e9),
-                   "tiles": {"rows": by, "z_depth": kc, "cells_per_thread": vec, "staged_planes": run_stages,
+        "config": workload_config(wl, world),
+        "bench_step": "one complete solve (all time steps) from resident initial fields",
+        "kernel": {"tiles": {"rows": by, "z_depth": kc, "cells_per_thread": vec, "staged_planes": run_stages,
                              "kernel": kernel},
                    "coefficients": (f"material index: {solver.material_count()} distinct (Ca, Cb, Da, Db) tuples, "
                                     "one byte per node + table; per-cell arrays given at the API" if mat else
-                                    "four per-cell FP32 arrays"),
-                   "parallelism": f"replicas x{world}"},
+                                    "four per-cell FP32 arrays")},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src,
                      "traffic": (tpc * cells) if tpc else None,
@@ -417,46 +431,46 @@ def run_ours(args, wl, world, rank, local):
         "e2e_graph": graph_e2e,
         "e2e": {"value": e2e_value, "unit": "Mcell-updates/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3 / args.steps, "result_ok": result_ok,
+                "path": "headline: the solver C ABI (ptk_solver_set_fields / set_coefficients / set_source, run, "
+                        "get_fields) with pinned host buffers, the call sequence of a C or C++ caller of this "
+                        "library; e2e_graph is the reference-facing PTask graph API with pageable arrays, as "
+                        "the reference's driver passes them",
                 "phases_ms_per_step": {k: v / args.steps for k, v in phase_ms.items()}},
         "gpu_launches": int(launches),
         "clocks": clk,
     }
+    solver.close()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample(prob, shape)
+    if world == 1 and not args.no_served and args.workload == "plain256":
+        # The workload's other half: batched and served solves/s and p50/p99 against every plain arm.
+        line["served"] = served_subrecords(args, rank, local)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    solver.close()
     dist.close()
     return 0
 
 
-def run_served(args, kind, world, rank, local):
-    """Batched (all requests at t=0) or served (Poisson arrivals) FDTD: continuous batching against
-    plain one-at-a-time dispatch of the same requests."""
+def serve_arms(reqs, scale: float, rows: int, *, cb_runs: int = 1, cb_warmup: int = 0, graph_arms=("fused", "taskwise"),
+               local: int = 0) -> dict:
+    """Serve one request set with continuous batching and with every plain one-at-a-time arm.
+
+    Arms, all on the same seeded requests and arrival times:
+      continuous      ptk_server: requests admitted as they arrive and fit the HBM budget, every active
+                      instance advanced by one persistent step launch per time step
+      plain_fused     the same server with one slot (max_active = 1): our best single-instance path
+      plain_graph_fused     one PTask FDTD graph per request shape, one request at a time: push the
+                      coefficients and fields, Graph::Run of the cyclic graph lowered to the fused loop,
+                      pull six fields (graphfdtd.cpp:1076-1125 is the loop this mirrors)
+      plain_graph_taskwise  the same, with the H and E tasks dispatched one by one per iteration by the
+                      scheduler (the reference's dispatch model)
+    """
     import ptask_gb300 as P
     from ptask_gb300 import _lib
-    from ptask_gb300.serve import Server, batched_instances, graph_dispatch, poisson_trace
+    from ptask_gb300.serve import Server, graph_dispatch
 
-    _lib.call("ptk_runtime_init", local)
-    if kind == "batched":
-        reqs = batched_instances(64, seed=4 + rank)
-        scale = 0.0
-        desc = ("batched FDTD: 64 instances in one persistent fused launch per step, edges per axis uniform "
-                "in [32,192], steps uniform in [100,2000], 1-8 dielectric boxes, seeded sources, FP32")
-    else:
-        n = args.requests
-        reqs = poisson_trace(n, rate=args.rate, seed=5 + rank)
-        scale = 1.0
-        trace = ("the workload's 20k-request trace" if n == 20000 else
-                 "the workload's 20k-request trace shortened")
-        desc = (f"served FDTD: Poisson arrivals {args.rate:g} req/s, {n} requests ({trace}"
-                f"{'' if args.rate == 200.0 else '; the workload offers 200 req/s, this rate is below saturation'}), "
-                "cube edge log-uniform in [24,256], steps uniform in [50,1000], FP32, admission by HBM budget")
     cells = sum(r.cell_updates for r in reqs)
-    # Staged tile shape per workload, as measured on GB300 (same box, alternating runs): the batched
-    # mix (x extents 32-192) runs 3.6 % faster on 7-row, 64-wide tiles; the served mix (cubes up to
-    # 256) 17 % faster on the server's default 11-row, 128-wide tiles.
-    rows = args.server_rows or (7 if kind == "batched" else 0)
+    peak, peak_src = hbm_peak()
 
     def serve(max_active):
         with Server(max_active=max_active, chunk_steps=32, persistent=True, tile_rows=rows) as s:
@@ -470,50 +484,112 @@ def run_served(args, kind, world, rank, local):
             st["pool_trims"] = _lib.lib().ptk_pool_trim_count() - t0
             return st
 
-    for _ in range(args.warmup if kind == "batched" else 0):
+    def arm_of(wall, p50, p99, chunk_dev=None):
+        a = {"solves_per_s": len(reqs) / wall, "mcell_updates_per_s": cells / wall / 1e6, "wall_s": wall,
+             "p50_latency_s": p50, "p99_latency_s": p99}
+        if chunk_dev:
+            a["frac_of_peak_over_device_time"] = BYTES_PER_CELL_MAT * cells / chunk_dev / 1e9 / peak
+        return a
+
+    for _ in range(cb_warmup):
         serve(0)
     clocks = ClockSampler(local)
     clocks.start()
-    runs = [serve(0) for _ in range(args.steps)]
+    runs = [serve(0) for _ in range(max(1, cb_runs))]
     clk = clocks.stop()
+    best = min(runs, key=lambda st: st["wall_s"])
+    wall = statistics.median(st["wall_s"] for st in runs)
+    cont = arm_of(wall, best["p50_latency_s"], best["p99_latency_s"], best["chunk_device_s"])
+    cont.update({"peak_active": best["peak_active"], "peak_bytes": best["peak_bytes"],
+                 "chunks": best["chunks"], "graph_captures": best["graph_captures"],
+                 "pool_trims": best["pool_trims"], "admit_waits": best["admit_waits"],
+                 "wall_breakdown_s": {k: best[k] for k in ("wall_s", "chunk_device_s", "admit_s", "retire_s",
+                                                           "schedule_s")}})
     plain = serve(1)
-    pgraph = None if args.no_plain_graph else graph_dispatch(reqs, scale, mode="taskwise")
-    best = min(runs, key=lambda s: s["wall_s"])
-    wall = statistics.median(s["wall_s"] for s in runs)
-    value = len(reqs) / wall
+    out = {"requests": len(reqs), "cell_updates": cells, "tile_rows": rows or 11,
+           "tile_width": 64 if rows in (7, 23) else 128, "continuous": cont,
+           "plain_fused": arm_of(plain["wall_s"], plain["p50_latency_s"], plain["p99_latency_s"],
+                                 plain["chunk_device_s"]),
+           "gpu_launches": int(best["launches"]), "clocks": clk,
+           "roofline_basis": "49 algorithmic bytes per cell update (material index) over the device time of the "
+                             "replayed chunks (every step launch, faces, advances) of the whole request set; "
+                             f"peak {peak:.1f} GB/s ({peak_src})"}
+    for mode in graph_arms:
+        g = graph_dispatch(reqs, scale, mode=mode)
+        out[f"plain_graph_{mode}"] = arm_of(g["wall_s"], g["p50_latency_s"], g["p99_latency_s"])
+    for name in ["plain_fused"] + [f"plain_graph_{m}" for m in graph_arms]:
+        out[f"speedup_vs_{name}"] = cont["solves_per_s"] / out[name]["solves_per_s"]
+    return out
+
+
+def batched_desc():
+    return ("batched FDTD: 64 instances in one persistent fused launch per step, edges per axis uniform in "
+            "[32,192], steps uniform in [100,2000], 1-8 dielectric boxes, seeded sources, FP32")
+
+
+def served_desc(n, rate):
+    trace = "the workload's 20k-request trace" if n == 20000 else "the workload's 20k-request trace shortened"
+    return (f"served FDTD: Poisson arrivals {rate:g} req/s, {n} requests ({trace}"
+            f"{'' if rate == 200.0 else '; the workload offers 200 req/s, this rate is below saturation'}), "
+            "cube edge log-uniform in [24,256], steps uniform in [50,1000], FP32, admission by HBM budget")
+
+
+# Staged tile shape per workload, as measured on GB300 (same box, alternating runs): the batched mix
+# (x extents 32-192) runs 3.6 % faster on 7-row, 64-wide tiles; the served mix (cubes up to 256) 17 %
+# faster on the server's default 11-row, 128-wide tiles.
+def default_rows(kind: str) -> int:
+    return 7 if kind == "batched" else 0
+
+
+def served_subrecords(args, rank: int, local: int) -> dict:
+    """Compact batched and served records for the default bench line (one run of every arm)."""
+    from ptask_gb300.serve import batched_instances, poisson_trace
+    out = {}
+    reqs = batched_instances(64, seed=4 + rank)
+    out["batched"] = {"workload": batched_desc(),
+                      **serve_arms(reqs, 0.0, args.server_rows or default_rows("batched"), cb_warmup=1, local=local)}
+    for key, rate in (("served", 200.0), ("served_below_saturation", args.subsat_rate)):
+        reqs = poisson_trace(args.served_requests, rate=rate, seed=5 + rank)
+        out[key] = {"workload": served_desc(args.served_requests, rate), "rate_req_per_s": rate,
+                    **serve_arms(reqs, 1.0, args.server_rows or default_rows("served"), local=local)}
+    return out
+
+
+def run_served(args, kind, world, rank, local):
+    """--workload batched|served: batched (all requests at t=0) or served (Poisson arrivals) FDTD,
+    continuous batching against every plain one-at-a-time arm on the same requests."""
+    from ptask_gb300 import _lib
+    from ptask_gb300.serve import batched_instances, poisson_trace
+
+    _lib.call("ptk_runtime_init", local)
+    if kind == "batched":
+        reqs, scale, desc = batched_instances(64, seed=4 + rank), 0.0, batched_desc()
+    else:
+        reqs, scale, desc = poisson_trace(args.requests, rate=args.rate, seed=5 + rank), 1.0, served_desc(
+            args.requests, args.rate)
+    rows = args.server_rows or default_rows(kind)
+    arms = () if args.no_plain_graph else ("fused", "taskwise")
+    rec = serve_arms(reqs, scale, rows, cb_runs=args.steps, cb_warmup=args.warmup if kind == "batched" else 0,
+                     graph_arms=arms, local=local)
+    cont = rec["continuous"]
+    peak, peak_src = hbm_peak()
     line = {
-        "metric": f"FDTD {kind} solves/s", "value": value, "unit": "solves/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1e3, "higher_is_better": True,
+        "metric": f"FDTD {kind} solves/s", "value": cont["solves_per_s"], "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": cont["wall_s"] * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded request generator)",
-        "config": {"workload": desc, "requests": len(reqs), "cell_updates": cells,
-                   "tile_rows": rows or 11, "tile_width": 64 if rows in (7, 23) else 128,
+        "config": {"workload": desc, "requests": len(reqs), "cell_updates": rec["cell_updates"],
+                   "tile_rows": rec["tile_rows"], "tile_width": rec["tile_width"],
                    "bench_step": "serve the whole request set", "l2": "working set larger than L2"},
-        "mcell_updates_per_s": cells / wall / 1e6,
-        "p50_latency_s": best["p50_latency_s"], "p99_latency_s": best["p99_latency_s"],
-        "peak_active": best["peak_active"], "peak_bytes": best["peak_bytes"],
-        "wall_breakdown_s": {k: best[k] for k in ("wall_s", "chunk_device_s", "admit_s", "retire_s", "schedule_s")},
-        "chunks": best["chunks"], "graph_captures": best["graph_captures"], "pool_trims": best["pool_trims"],
-        "admit_waits": best["admit_waits"],
-        "plain": {"solves_per_s": len(reqs) / plain["wall_s"], "mcell_updates_per_s": cells / plain["wall_s"] / 1e6,
-                  "p50_latency_s": plain["p50_latency_s"], "p99_latency_s": plain["p99_latency_s"],
-                  "wall_s": plain["wall_s"]},
-        "speedup_vs_plain": (len(reqs) / wall) / (len(reqs) / plain["wall_s"]),
-        "plain_graph": None if pgraph is None else {
-            "dispatch": "one PTask FDTD graph per request shape, one request at a time, H and E tasks "
-                        "dispatched per iteration by the scheduler; inputs pushed, six fields pulled",
-            "solves_per_s": pgraph["solves"] / pgraph["wall_s"],
-            "mcell_updates_per_s": cells / pgraph["wall_s"] / 1e6,
-            "p50_latency_s": pgraph["p50_latency_s"], "p99_latency_s": pgraph["p99_latency_s"],
-            "wall_s": pgraph["wall_s"]},
-        "speedup_vs_plain_graph": None if pgraph is None else (len(reqs) / wall) / (pgraph["solves"] / pgraph["wall_s"]),
-        "roofline": {"bound": "hbm", "unit": "GB/s", "peak": hbm_peak()[0], "peak_source": hbm_peak()[1],
-                     "achieved": BYTES_PER_CELL_MAT * cells / best["chunk_device_s"] / 1e9,
-                     "frac": BYTES_PER_CELL_MAT * cells / best["chunk_device_s"] / 1e9 / hbm_peak()[0],
-                     "traffic": None,
-                     "basis": "whole request set: 49 algorithmic bytes per cell update (material index) over the "
-                              "device time of the replayed chunks (all step launches, faces, advances)"},
-        "gpu_launches": int(best["launches"]),
-        "clocks": clk,
+        "mcell_updates_per_s": cont["mcell_updates_per_s"],
+        "p50_latency_s": cont["p50_latency_s"], "p99_latency_s": cont["p99_latency_s"],
+        "arms": {k: rec[k] for k in rec if k.startswith("plain_") or k == "continuous"},
+        "speedups": {k: v for k, v in rec.items() if k.startswith("speedup_vs_")},
+        "roofline": {"bound": "hbm", "unit": "GB/s", "peak": peak, "peak_source": peak_src,
+                     "achieved": cont["frac_of_peak_over_device_time"] * peak,
+                     "frac": cont["frac_of_peak_over_device_time"], "traffic": None,
+                     "basis": rec["roofline_basis"]},
+        "gpu_launches": rec["gpu_launches"],
+        "clocks": rec["clocks"],
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -541,7 +617,13 @@ def main() -> int:
     ap.add_argument("--no-graph-e2e", action="store_true",
                     help="plain workloads: skip the end-to-end run through the PTask graph API")
     ap.add_argument("--no-plain-graph", action="store_true",
-                    help="batched/served: skip the per-graph (task-wise) plain dispatch arm")
+                    help="batched/served: skip the two per-graph plain dispatch arms (fused and task-wise)")
+    ap.add_argument("--no-served", action="store_true",
+                    help="default line: leave out the batched and served sub-records")
+    ap.add_argument("--served-requests", type=int, default=300,
+                    help="default line: requests in each served sub-record's trace")
+    ap.add_argument("--subsat-rate", type=float, default=60.0,
+                    help="default line: arrival rate of the below-saturation served sub-record, requests/s")
     args = ap.parse_args()
     world, rank, local = dist_env()
     if args.workload in ("batched", "served") and args.impl == "ours":

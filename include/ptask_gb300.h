@@ -226,19 +226,22 @@ int ptk_fdtd_solve(const ptk_fdtd_params *p, float *const fields[6], const float
                    const float *Cb, const float *Da, const float *Db, int si, int sj, int sk,
                    const float *wave, int nwave, int steps, float *ms);
 
-/* Allocation-free solve.  No counterpart in the reference: it exists for callers that cannot let a
- * library allocate GPU memory -- code running while another component captures the stream into a CUDA
- * graph (cudaMalloc is not allowed there), plugins whose host application owns all device memory, and
- * latency-critical loops that must not risk an allocation failure mid-run.
+/* Allocation-free solve.  No counterpart in the reference.  It is for callers that must not have a
+ * library allocate GPU memory: a plugin whose host application hands out all device memory from its
+ * own arena and budget (a private cudaMalloc bypasses that accounting and can fail when the arena
+ * holds the rest of the GPU), and latency-critical loops that cannot take cudaMalloc / cudaFree
+ * (they may synchronise the device, and their latency is unbounded).
  * fields[6] (device, reference layout) are advanced `steps` steps in place with the fused kernel;
  * Ca..Db (device, Nx*Ny*Nz each) may all be NULL for vacuum coefficients; wave (device) may be NULL.
  * stream NULL means the current device's default stream.  All scratch lives in one static device
  * array of ptk_fdtd_static_scratch_bytes() bytes (48 MiB) that every GPU loading the library holds
- * until exit; grids needing more (padded node count roundup(Nx+1,32)*(Ny+1)*(Nz+1) above about 786k)
- * are rejected with PTK_ERR_BUDGET.  The first call on a device looks up the array's address
- * (cudaGetSymbolAddress) with that device current: make it before any stream capture.  Calls share
- * the array, which keeps the previous call's contents (each call clears what it uses): calls whose
- * GPU work overlaps race and must be serialised by the caller. */
+ * until exit: cubes up to 89^3 fit (padded node count roundup(Nx+1,32)*(Ny+1)*(Nz+1) up to 786,424);
+ * larger grids are rejected with PTK_ERR_BUDGET before any device work.  No cudaMalloc, cudaFree or
+ * other allocating routine is called.  The first call on a device looks up the array's address
+ * (cudaGetSymbolAddress) with that device current and keeps it: make that call before any stream
+ * capture, and make no call on a device after cudaDeviceReset.  Calls share the array, which keeps
+ * the previous call's contents (each call clears what it uses): calls whose GPU work overlaps race
+ * and must be serialised by the caller. */
 int ptk_fdtd_solve_static(const ptk_fdtd_params *p, float *const fields[6], const float *Ca,
                           const float *Cb, const float *Da, const float *Db, int si, int sj, int sk,
                           const float *wave, int nwave, int steps, void *stream);

@@ -8,6 +8,8 @@ package; the product (ptask_gb300) never does.
   step_ext_f64   FP64 twin of step_ext_f32
   ref_fdtd_cpu   the reference's own fdtd_cpu compiled from its sources into oracle/_ref
                  (only where the reference tree was present at build time)
+  problem_generate  the benchmark's seeded problem generator, restated here (bit-equal to
+                 ptask_gb300's; pinned by tests) so that the CPU baseline loads nothing of the product
 """
 from __future__ import annotations
 
@@ -27,6 +29,14 @@ class Params(C.Structure):
     _fields_ = [("Nx", C.c_int), ("Ny", C.c_int), ("Nz", C.c_int),
                 ("Cx", C.c_float), ("Cy", C.c_float), ("Cz", C.c_float),
                 ("eps0", C.c_float), ("mu0", C.c_float), ("c0", C.c_float), ("Dt", C.c_float)]
+
+
+class ProblemDesc(C.Structure):
+    """Description of a seeded problem (same layout as ptk_problem_desc)."""
+    _fields_ = [("Nx", C.c_int), ("Ny", C.c_int), ("Nz", C.c_int), ("n_boxes", C.c_int),
+                ("eps_min", C.c_float), ("eps_max", C.c_float), ("box_min", C.c_int),
+                ("box_max", C.c_int), ("courant", C.c_float), ("steps", C.c_int),
+                ("source_mode", C.c_int), ("seed", C.c_uint64)]
 
 
 def params_from(p) -> Params:
@@ -51,6 +61,8 @@ def _oracle():
         L.oracle_ext_f64.argtypes = [C.POINTER(V), C.POINTER(V)] + [V] * 4 + [
             C.c_int, C.POINTER(Params), C.c_int, C.c_int, C.c_int, V, C.c_int]
         L.oracle_threads.restype = C.c_int
+        L.oracle_problem_generate.argtypes = [C.POINTER(ProblemDesc), C.POINTER(Params)] + [V] * 4 + [
+            C.POINTER(C.c_int)] * 3 + [V]
         _o = L
     return _o
 
@@ -121,6 +133,35 @@ def ref_fdtd_cpu(fields, steps: int, params, blocks: int = 0) -> list[np.ndarray
         rc = _ref().ref_fdtd_cpu(*[a.ctypes.data for a in out], steps, P)
     assert rc == 0, rc
     return out
+
+
+FIELD_GROWS = ((1, 0, 0), (0, 1, 0), (0, 0, 1), (0, 1, 1), (1, 0, 1), (1, 1, 0))   # Hx..Ez: +1 on x, y, z
+
+
+def zero_fields(nx: int, ny: int, nz: int) -> list[np.ndarray]:
+    """Six zero fields in the reference's dense layout (C-ordered (d3, d2, d1), graphfdtd.cpp:68-86)."""
+    return [np.zeros((nz + gz, ny + gy, nx + gx), np.float32) for gx, gy, gz in FIELD_GROWS]
+
+
+class OracleProblem:
+    """A generated problem: params (FDTD_PARAMS layout), per-cell coefficients, source, waveform."""
+
+    def __init__(self, params, Ca, Cb, Da, Db, src, wave):
+        self.params, self.Ca, self.Cb, self.Da, self.Db, self.src, self.wave = params, Ca, Cb, Da, Db, src, wave
+
+
+def problem_generate(nx: int, ny: int, nz: int, *, n_boxes: int = 2, eps=(2.0, 6.0), box=(4, 16),
+                     courant: float = 0.5, steps: int = 100, source_mode: int = 1, seed: int = 1) -> OracleProblem:
+    """Same arguments and the same arrays as ptask_gb300.Problem.generate."""
+    d = ProblemDesc(nx, ny, nz, n_boxes, eps[0], eps[1], box[0], box[1], courant, steps, source_mode, seed)
+    p = Params()
+    Ca, Cb, Da, Db = (np.empty((nz, ny, nx), np.float32) for _ in range(4))
+    wave = np.zeros(max(steps, 1), np.float32)
+    si, sj, sk = C.c_int(), C.c_int(), C.c_int()
+    rc = _oracle().oracle_problem_generate(C.byref(d), C.byref(p), Ca.ctypes.data, Cb.ctypes.data, Da.ctypes.data,
+                                           Db.ctypes.data, C.byref(si), C.byref(sj), C.byref(sk), wave.ctypes.data)
+    assert rc == 0, rc
+    return OracleProblem(p, Ca, Cb, Da, Db, (si.value, sj.value, sk.value), wave[:steps])
 
 
 def normwise_error(got, ref) -> float:

@@ -20,6 +20,11 @@
  *                       figure.
  *   oracle_field_task_f32  one per-field task (graphfdtd.cpp:185-312), out of place, for the test
  *                       host-task library.
+ *   oracle_problem_generate  the benchmark's seeded problem generator (vacuum cavity with the
+ *                       reference's constants, graphfdtd.cpp:1357-1381, plus dielectric boxes, a
+ *                       Courant-number time step and a Gaussian source), restated independently of
+ *                       the product library so that the CPU baseline needs nothing from it.  Tests
+ *                       pin it bit for bit to ptk_problem_generate.
  *
  * Layouts are the reference's (Simple3DArray.h:33): element (i,j,k) of an array with extents
  * (d1,d2,d3) sits at i + j*d1 + k*d1*d2; the six fields have extents
@@ -315,4 +320,120 @@ int oracle_threads(void)
 #else
     return 1;
 #endif
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Seeded problem generator.  Same description and the same numbers as ptk_problem_generate:   */
+/* a splitmix64 stream draws the boxes (edges, positions, eps_r) and the source position; the  */
+/* vacuum constants are the reference's cavity (graphfdtd.cpp:1357-1361).  Every expression is */
+/* evaluated in the type and order the description below gives, so the arrays are bit-equal.   */
+/* ------------------------------------------------------------------------------------------ */
+#include <math.h>
+
+typedef struct oracle_problem_desc {   /* same layout as ptk_problem_desc */
+    int Nx, Ny, Nz;
+    int n_boxes;
+    float eps_min, eps_max;
+    int box_min, box_max;
+    float courant;
+    int steps;
+    int source_mode;    /* 0 none, 1 centre, 2 seeded interior node */
+    uint64_t seed;
+} oracle_problem_desc;
+
+static uint64_t sm64_next(uint64_t *s)
+{
+    uint64_t z = (*s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+/* uniform double in [0, 1) from the top 53 bits */
+static double sm64_u01(uint64_t *s) { return (double)(sm64_next(s) >> 11) * (1.0 / 9007199254740992.0); }
+
+/* uniform integer in [a, b] */
+static int sm64_range(uint64_t *s, int a, int b)
+{
+    int v;
+    if (b <= a) return a;
+    v = a + (int)(sm64_u01(s) * (double)(b - a + 1));
+    return v > b ? b : v;
+}
+
+int oracle_problem_generate(const oracle_problem_desc *d, oracle_params *p, float *Ca, float *Cb, float *Da,
+                            float *Db, int *si, int *sj, int *sk, float *wave)
+{
+    const float Lx = 0.05f, Ly = 0.04f, Lz = 0.03f, pi = 3.1415f;
+    uint64_t s;
+    int b, a, n, Nx, Ny, Nz, i = -1, j = -1, k = -1;
+    size_t c, ncell;
+    float *epsr;
+    double cx, cy, cz;
+    if (!d || !p || d->Nx < 1 || d->Ny < 1 || d->Nz < 1 || d->steps < 0 || d->n_boxes < 0) return 1;
+    Nx = d->Nx; Ny = d->Ny; Nz = d->Nz;
+    p->Nx = Nx; p->Ny = Ny; p->Nz = Nz;
+    p->Cx = (float)Nx / Lx;
+    p->Cy = (float)Ny / Ly;
+    p->Cz = (float)Nz / Lz;
+    p->eps0 = 8.8541878e-12f;
+    p->mu0 = 4e-7f * pi;
+    p->c0 = 299792458.0f;
+    cx = p->Cx; cy = p->Cy; cz = p->Cz;
+    p->Dt = (float)((double)d->courant / ((double)p->c0 * sqrt(cx * cx + cy * cy + cz * cz)));
+
+    ncell = (size_t)Nx * Ny * Nz;
+    epsr = (float *)malloc(ncell * sizeof(float));
+    if (!epsr) return 2;
+    for (c = 0; c < ncell; ++c) epsr[c] = 1.0f;
+    s = d->seed;
+    for (b = 0; b < d->n_boxes; ++b) {   /* later boxes overwrite earlier ones */
+        const int N[3] = {Nx, Ny, Nz};
+        int lo[3], hi[3], x, y, z;
+        float e;
+        for (a = 0; a < 3; ++a) {
+            int size = sm64_range(&s, d->box_min, d->box_max);
+            if (size < 1) size = 1;
+            if (size > N[a]) size = N[a];
+            lo[a] = sm64_range(&s, 0, N[a] - size);
+            hi[a] = lo[a] + size;
+        }
+        e = (float)(d->eps_min + (double)(d->eps_max - d->eps_min) * sm64_u01(&s));
+        for (z = lo[2]; z < hi[2]; ++z)
+            for (y = lo[1]; y < hi[1]; ++y)
+                for (x = lo[0]; x < hi[0]; ++x) epsr[IDX(x, y, z, Nx, Ny)] = e;
+    }
+    if (d->source_mode != 0 && Nx >= 2 && Ny >= 2) {
+        if (d->source_mode == 1) {
+            i = Nx / 2; j = Ny / 2; k = Nz / 2;
+        } else {
+            i = sm64_range(&s, 1, Nx - 1);
+            j = sm64_range(&s, 1, Ny - 1);
+            k = sm64_range(&s, 0, Nz - 1);
+        }
+    }
+    if (si) *si = i;
+    if (sj) *sj = j;
+    if (sk) *sk = k;
+    {
+        const float ch = p->Dt / p->mu0;
+        for (c = 0; c < ncell; ++c) {
+            if (Ca) Ca[c] = 1.0f;
+            if (Cb) Cb[c] = p->Dt / (p->eps0 * epsr[c]);
+            if (Da) Da[c] = 1.0f;
+            if (Db) Db[c] = ch;
+        }
+    }
+    free(epsr);
+    if (wave) {   /* Gaussian pulse exp(-((n - t0)/tw)^2), tw = steps/8 clamped to [2, 20], t0 = 3 tw */
+        double tw = d->steps / 8.0, t0;
+        if (tw > 20.0) tw = 20.0;
+        if (tw < 2.0) tw = 2.0;
+        t0 = 3.0 * tw;
+        for (n = 0; n < d->steps; ++n) {
+            const double x = ((double)n - t0) / tw;
+            wave[n] = (i >= 0) ? (float)exp(-x * x) : 0.0f;
+        }
+    }
+    return 0;
 }

@@ -23,6 +23,10 @@ RTSRC = PKG / "runtime"
 APPS = PKG / "apps"
 BUILD = PKG / "_build"
 INCLUDE = ROOT / "include"
+# Root of the reference project's source tree (read only; only the oracle recipe and the drop-in
+# compile test use it, and only where it exists).  One environment variable, shared with
+# oracle/Makefile and tests/test_dropin.py.
+REFERENCE = Path(os.environ.get("PTASK_REFERENCE", "/root/reference"))
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
@@ -138,9 +142,9 @@ def build_oracle(verbose: bool = False) -> None:
     src = odir / "fdtd_oracle.c"
     if _newer(lib, [src]):
         _run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp",
-              str(src), "-o", str(lib)])
-    if Path("/root/reference/ptaskUnitTest/graphfdtd.cpp").exists():
-        _run(["make", "-s", "-C", str(odir), "ref"])
+              str(src), "-o", str(lib), "-lm"])
+    if (REFERENCE / "ptaskUnitTest" / "graphfdtd.cpp").exists():
+        _run(["make", "-s", "-C", str(odir), "ref", f"REF={REFERENCE / 'ptaskUnitTest'}"])
     if verbose:
         print(f"built {lib}")
 

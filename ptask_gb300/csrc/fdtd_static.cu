@@ -1,19 +1,23 @@
 // fdtd_static.cu -- an FDTD solve that allocates no device memory.
 //
-// Some callers cannot let a library allocate GPU memory: code that runs while another component is
-// capturing the stream into a CUDA graph (cudaMalloc is not allowed during a global capture),
-// plugins whose host application hands out all device memory through its own allocator and budget,
-// and latency-critical loops that must not risk an allocation failure or a pool-growth stall in the
-// middle of a time step.  ptk_fdtd_solve_static serves them: the caller passes its six fields and
-// coefficients in device memory, and every intermediate the fused step kernel needs (the padded
-// ping-pong fields, padded coefficients and the one-entry work list) lives in one file-scope
+// Who this is for: callers that must not have a library allocate GPU memory behind their back.  A
+// plugin or solver component inside a larger application often gets all of its device memory from
+// the host application's own arena, sized against a budget; a private cudaMalloc bypasses that
+// accounting and can fail once the arena holds the rest of the GPU.  A latency-critical loop cannot
+// take cudaMalloc / cudaFree either: they may synchronise the device and their latency is unbounded.
+// ptk_fdtd_solve_static serves both: the caller passes its six fields and coefficients in device
+// memory, and every intermediate the fused step kernel needs (the padded ping-pong fields, padded
+// coefficients, the instance descriptor and the one-entry work list) lives in one file-scope
 // __device__ array of fixed size.  It calls no cudaMalloc, cudaFree or other allocating routine.
 //
 // Costs and rules, for the user:
-//   * Every GPU that loads this library holds kStaticScratchBytes of device memory until the
-//     process exits (the array is part of the module image).
+//   * Every GPU that loads this library holds kStaticScratchBytes (48 MiB) of device memory until
+//     the process exits (the array is part of the module image).  Cubes up to 89^3 fit (padded
+//     nodes roundup(Nx+1,32) * (Ny+1) * (Nz+1) up to 786,424); larger grids are rejected.
 //   * The array's device address is looked up once per device (cudaGetSymbolAddress) by the first
-//     call on that device, with that device current; make that first call before any stream capture.
+//     call on that device, with that device current, and kept for the life of the process: make
+//     that first call before any stream capture, and do not call again on a device after
+//     cudaDeviceReset (the kept address would name freed memory).
 //   * All calls share the one array and it keeps the previous call's contents: the regions a call
 //     uses are cleared at its start.  Calls whose GPU work overlaps (different streams, no ordering)
 //     race on the array; serialise them.
@@ -24,8 +28,8 @@
 
 namespace ptk {
 
-// 48 MiB: grids whose padded node count (roundup(Nx+1,32) * (Ny+1) * (Nz+1)) is at most about
-// 786k, e.g. 64x64x64 or 96x64x48.
+// 48 MiB: 16 padded arrays and a 512-byte header, i.e. grids whose padded node count
+// (roundup(Nx+1,32) * (Ny+1) * (Nz+1)) is at most 786,424: cubes up to 89^3, or e.g. 96x64x48.
 constexpr size_t kStaticScratchBytes = 48ull << 20;
 constexpr size_t kStaticAlign = 256;
 

@@ -7,6 +7,7 @@ passed as char*).  The program is not run here (no GPU in this container, and th
 absent where the GPU tests run); tests/test_graph_gpu.py runs the same graph structure, built by
 ptask_gb300/runtime/fdtd_graph.cpp through the same API calls, on the GPU.
 """
+import os
 import shutil
 import subprocess
 from pathlib import Path
@@ -15,7 +16,7 @@ import pytest
 
 from conftest import ROOT
 
-REF = Path("/root/reference/ptaskUnitTest")
+REF = Path(os.environ.get("PTASK_REFERENCE", "/root/reference")) / "ptaskUnitTest"
 BUILD = ROOT / "ptask_gb300" / "_build"
 
 

@@ -253,6 +253,27 @@ def test_full_size_full_length_matches_oracle(full_problem):
     assert_parity(got, ref, "256^3 x 1000")
 
 
+LARGE = (512, 512, 384)
+
+
+def test_large_config_full_length_matches_oracle():
+    """The large single-GPU workload itself (512x512x384, 32 seeded dielectric boxes, 500 steps from
+    zero fields, as the benchmark's `--workload large` generates it) with the autotuned tiles, bit
+    for bit against the FP32 oracle (about 30 s of host time on 16 cores)."""
+    pr = P.Problem.generate(*LARGE, n_boxes=32, eps=(1, 10), box=(8, 64), steps=500, seed=2)
+    f = P.zero_fields(*LARGE)
+    with P.Solver(pr.params) as s:
+        s.set_tiles(*P.tuned_tiles(*LARGE))
+        s.set_fields(f)
+        s.set_problem(pr)
+        s.run(500)
+        stages, mat = s.kernel()
+        assert stages > 0 and mat, "the large workload runs the staged material-index kernel"
+        got = s.get_fields()
+    ref = oracle.step_ext_f32(f, 500, pr.params, pr.Ca, pr.Cb, pr.Da, pr.Db, pr.src, pr.wave)
+    assert_parity(got, ref, "512x512x384 x 500")
+
+
 def test_full_size_tiling_and_chunking_invariance(full_problem):
     pr = full_problem
     f = P.zero_fields(*FULL)

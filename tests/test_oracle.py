@@ -113,3 +113,25 @@ def test_pec_walls_stay_fixed():
     Ez0, Ez1 = f[5], out[5]          # (Nz, Ny+1, Nx+1)
     np.testing.assert_array_equal(Ez1[:, :, 0], Ez0[:, :, 0])
     np.testing.assert_array_equal(Ez1[:, :, -1], Ez0[:, :, -1])
+
+
+@pytest.mark.parametrize("shape,kw", [
+    ((256, 256, 256), dict(n_boxes=8, eps=(1.0, 10.0), box=(8, 64), steps=1000, source_mode=1, seed=2)),
+    ((512, 512, 384), dict(n_boxes=32, eps=(1.0, 10.0), box=(8, 64), steps=500, source_mode=1, seed=2)),
+    ((37, 29, 23), dict(n_boxes=3, eps=(1.0, 10.0), box=(4, 11), steps=75, source_mode=2, seed=400002)),
+    ((130, 24, 20), dict(n_boxes=4, eps=(1.0, 10.0), box=(8, 64), steps=20, source_mode=2, seed=5)),
+    ((1, 1, 1), dict(n_boxes=2, eps=(2.0, 6.0), box=(4, 16), steps=3, source_mode=1, seed=1)),
+    ((5, 1, 7), dict(n_boxes=0, steps=0, source_mode=0, seed=9)),
+])
+def test_oracle_problem_generator_is_the_products(shape, kw):
+    """The oracle's own copy of the seeded problem generator (used by the CPU baseline, which loads
+    nothing of the product) gives the same bits as ptk_problem_generate."""
+    a = P.Problem.generate(*shape, **kw)
+    b = oracle.problem_generate(*shape, **kw)
+    for f, _ in oracle.Params._fields_:
+        assert np.array(getattr(a.params, f)).tobytes() == np.array(getattr(b.params, f)).tobytes(), f
+    assert a.src == b.src
+    for x, y in zip((a.Ca, a.Cb, a.Da, a.Db, a.wave), (b.Ca, b.Cb, b.Da, b.Db, b.wave)):
+        assert x.shape == y.shape and np.array_equal(x.view(np.uint32), y.view(np.uint32))
+    for f, g in zip(P.zero_fields(*shape), oracle.zero_fields(*shape)):
+        assert f.shape == g.shape and f.dtype == g.dtype and not g.any()

@@ -140,3 +140,36 @@ def test_many_work_lists_evict_cached_graphs_and_stay_exact():
             ref, _ = alone(reqs[q])
             for f in range(6):
                 np.testing.assert_array_equal(got[f], ref[f], err_msg=f"request {q} field {P.FIELDS[f]}")
+
+
+@pytest.mark.parametrize("rows", [7, 0])
+def test_full_batched_set_matches_oracle(rows):
+    """The whole 64-instance batched workload (per-axis edges 32-192, 100-2000 steps, the set the
+    benchmark serves), run in one continuous-batching mix with the benchmark's 7-row, 64-wide tiles
+    and with the server's default 11-row, 128-wide ones.  A seeded subset of 8 instances, always
+    including the largest, is compared with the FP32 oracle (graphfdtd.cpp:314-340 restated) bit for
+    bit; every instance's checksums are compared with its fields."""
+    reqs = batched_instances(64, seed=4)
+    largest = max(range(len(reqs)), key=lambda q: reqs[q].cell_updates)
+    rng = np.random.default_rng(17 + rows)
+    pick = sorted({largest, *(int(q) for q in rng.choice(len(reqs), 7, replace=False))})
+    with Server(keep_results=True, chunk_steps=32, tile_rows=rows) as s:
+        tickets = [s.submit(r) for r in reqs]
+        s.run(time_scale=0)
+        st = s.stats()
+        assert st["completed"] == len(reqs) and st["peak_active"] == len(reqs)
+        fetched = {q: s.fetch(tickets[q]) for q in pick}
+        sums = {q: list(s.info(tickets[q]).checksum) for q in pick}
+    for q in pick:
+        r = reqs[q]
+        pr = P.Problem.generate(r.nx, r.ny, r.nz, n_boxes=r.n_boxes, eps=r.eps, box=r.box, steps=r.steps,
+                                source_mode=r.source_mode, seed=r.seed)
+        ref =oracle.step_ext_f32(P.zero_fields(r.nx, r.ny, r.nz), r.steps, pr.params, pr.Ca, pr.Cb, pr.Da, pr.Db,
+                                  pr.src, pr.wave)
+        for f in range(6):
+            got = fetched[q][f]
+            assert oracle.normwise_error(got, ref[f]) <= 1e-5
+            np.testing.assert_array_equal(got, ref[f], err_msg=f"instance {q} ({r.nx}x{r.ny}x{r.nz} x {r.steps}) "
+                                                               f"field {P.FIELDS[f]}")
+            f64 = got.astype(np.float64)
+            assert abs(sums[q][f] - f64.sum()) <= 1e-12 * max(np.abs(f64).sum(), 1e-300)
