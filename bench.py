@@ -563,7 +563,9 @@ def run_served(args, kind, world, rank, local):
 
     _lib.call("ptk_runtime_init", local)
     if kind == "batched":
-        reqs, scale, desc = batched_instances(64, seed=4 + rank), 0.0, batched_desc()
+        reqs, scale, desc = batched_instances(args.instances, seed=4 + rank), 0.0, batched_desc()
+        if args.instances != 64:
+            desc += f"; the first {args.instances} of its 64 instances"
     else:
         reqs, scale, desc = poisson_trace(args.requests, rate=args.rate, seed=5 + rank), 1.0, served_desc(
             args.requests, args.rate)
@@ -604,6 +606,8 @@ def main() -> int:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batched", "served"], default="plain256")
     ap.add_argument("--requests", type=int, default=1000, help="served workload: requests in the trace")
+    ap.add_argument("--instances", type=int, default=64,
+                    help="batched workload: serve the first N of its 64 seeded instances (profiling runs)")
     ap.add_argument("--rate", type=float, default=200.0,
                     help="served workload: Poisson arrival rate, requests/s (200: the workload's rate)")
     ap.add_argument("--server-rows", type=int, default=0,

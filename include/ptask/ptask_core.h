@@ -162,6 +162,17 @@ public:
     int GetInOutRoutingIndex() { return m_inout_idx; }
     BOOL IsInOutParameter() { return m_inout_idx >= 0; }
     BOOL IsSticky() { return m_type == STICKY_PORT; }
+    // Dependent-accelerator binding (port.h:1185-1248): the block bound to this port of a host task
+    // is materialised in the memory space of the task's dependent accelerator (a device pointer)
+    // instead of host memory.  nIndex picks one of the task's dependent accelerators.
+    void BindDependentAccelerator(ACCELERATOR_CLASS cls, int nIndex)
+    {
+        m_dep_class = cls;
+        m_dep_index = nIndex;
+    }
+    BOOL HasDependentAcceleratorBinding() { return m_dep_class != ACCELERATOR_CLASS_UNKNOWN; }
+    int GetDependentAcceleratorIndex() { return m_dep_index; }
+    ACCELERATOR_CLASS GetDependentAcceleratorClass() { return m_dep_class; }
     void SetMetaFunction(METAFUNCTION f) { m_meta = f; }
     METAFUNCTION GetMetaFunction() { return m_meta; }
     void SetSticky(BOOL b) { m_sticky_flag = b; }
@@ -173,6 +184,8 @@ public:
     Channel *GetChannel(UINT i);
 
     // ---- runtime side ----
+    ACCELERATOR_CLASS m_dep_class = ACCELERATOR_CLASS_UNKNOWN;   // dependent binding, if any
+    int m_dep_index = -1;
     std::vector<Channel *> m_in;         // channels feeding an input-side port
     std::vector<Channel *> m_out;        // channels fed by an output port
     std::vector<Port *> m_ctl_targets;   // control propagation (BindControlPropagationPort)
@@ -287,6 +300,32 @@ public:
 // pointers, in parameter-index order.  (__stdcall has no meaning on the platforms this runs on.)
 typedef void (*LPFNHOSTTASK)(UINT nArguments, void **ppArguments);
 
+// Host tasks that use a dependent accelerator (hosttask.h:45-144).  Arguments bound to ports with a
+// dependent binding are device pointers (pbIsDependentBinding[i] TRUE, pvDeviceBindings[i] the
+// device's ordinal as a pointer-sized integer); the others are host pointers.  pDeps / the
+// context's pDependentDevices list the dependent devices (one: the runtime's GPU).
+typedef void (*LPFNDEPHOSTTASK)(UINT nArguments, void **ppArguments, BOOL *pbIsDependentBinding,
+                                void **pvDeviceBindings, UINT nDeps, void **pDeps);
+
+// Descriptor form, chosen when the task asked for platform-specific objects
+// (BindDependentAcceleratorClass(..., bRequestDependentPSObjects = TRUE)).  Same member order and
+// types as the reference's DEPENDENTCONTEXT, so entry points written for it read it unchanged;
+// pStreams[0] is the CUDA stream (cudaStream_t) the task's work must be ordered on.
+typedef struct _dependent_context_t {
+    UINT cbDependentContext;       // sizeof(DEPENDENTCONTEXT)
+    UINT nArguments;
+    UINT nDependentAccelerators;
+    UINT uiReserved0;
+    void **ppArguments;
+    Datablock **ppDatablocks;      // the block behind each argument
+    BOOL *pbIsDependentBinding;
+    void **pvDeviceBindings;
+    void **pDependentDevices;
+    void **pStreams;
+    char *lpszTaskName;
+} DEPENDENTCONTEXT, *LPDEPENDENTCONTEXT;
+typedef void (*LPFNDEPHOSTTASKEX)(LPDEPENDENTCONTEXT);
+
 // A (file, entry) pair resolved to a linked native kernel, or to a host function exported by a
 // shared library (CompiledKernel.h; hostaccelerator.cpp:328-380 for the host case).
 class CompiledKernel {
@@ -318,6 +357,15 @@ public:
     {
         return m_kernel && m_kernel->IsHost() ? ACCELERATOR_CLASS_HOST : ACCELERATOR_CLASS_CUDA;
     }
+    // Dependent accelerators of a host task (task.h:768-800): the scheduler gives the task an
+    // accelerator of class `cls` besides the host.  With bRequestDependentPSObjects the entry point
+    // has the LPFNDEPHOSTTASKEX form and receives streams; otherwise LPFNDEPHOSTTASK.  Only the
+    // CUDA class, one instance, is supported (one GPU per runtime); anything else fails.
+    BOOL BindDependentAcceleratorClass(ACCELERATOR_CLASS cls, int nRequiredInstances, BOOL bRequestDependentPSObjects);
+    int GetDependentBindingClassCount() { return m_dep_class == ACCELERATOR_CLASS_UNKNOWN ? 0 : 1; }
+    BOOL HasDependentAcceleratorBindings() { return GetDependentBindingClassCount() > 0; }
+    BOOL DependentBindingsRequirePSObjects() { return m_dep_ps; }
+    ACCELERATOR_CLASS GetDependentAcceleratorClass(int) { return m_dep_class; }
     Graph *GetGraph() { return m_graph; }
     CompiledKernel *GetCompiledKernel() { return m_kernel; }
     UINT GetInputPortCount() { return (UINT)m_inputs.size(); }
@@ -339,6 +387,8 @@ public:
     void *m_step_counter = nullptr;   // device int used by kernels that index a waveform by step
     CyclePlan *m_loop_top = nullptr;     // this task heads a general-iteration loop
     CyclePlan *m_loop_bottom = nullptr;  // this task owns the loop's MF_GENERAL_ITERATOR port
+    ACCELERATOR_CLASS m_dep_class = ACCELERATOR_CLASS_UNKNOWN;   // dependent accelerator class
+    BOOL m_dep_ps = FALSE;               // entry point wants DEPENDENTCONTEXT (streams)
 
 private:
     Graph *m_graph;

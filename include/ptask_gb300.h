@@ -102,6 +102,11 @@ int ptk_memset(void *dst, int value, size_t bytes, void *stream);
 int ptk_stream_create(void **stream);
 int ptk_stream_destroy(void *stream);
 int ptk_stream_sync(void *stream);
+/* Wait for all work on the runtime's device (every stream).  Used around host tasks of the
+ * dependent form without streams (LPFNDEPHOSTTASK), which may launch work on any stream. */
+int ptk_device_sync(void);
+/* Ordinal of the runtime's CUDA device (the dependent device a host task is handed). */
+int ptk_device_ordinal(int *device);
 int ptk_event_create(void **event);
 int ptk_event_destroy(void *event);
 int ptk_event_record(void *event, void *stream);
@@ -325,6 +330,12 @@ int ptk_selftest_wait_expiry(int *error_word, float *elapsed_ms);
 /* Time candidate tile shapes for a grid of the given size on the current device and return the
  * fastest (cached per shape for the life of the process). */
 int ptk_autotune_tiles(int Nx, int Ny, int Nz, ptk_tile_config *best, float *best_ms_per_step);
+/* Tile shape without timing anything: the autotuner's choice when this process has tuned the
+ * shape already, else the TMA-staged material-index kernel with 11-row tiles, a 4-plane ring and
+ * the z depth that fills whole waves of resident CTAs best.  The PTask graph's loop lowering uses
+ * it, so that a graph built for one request does not pay for a full autotuning pass.  Needs the
+ * runtime to be initialised (the resident CTA count comes from the device). */
+int ptk_default_tiles(int Nx, int Ny, int Nz, ptk_tile_config *cfg);
 
 /* ============================== synthetic problems ============================================ */
 /* Seeded problem generator used by tests and benchmarks: vacuum plus axis-aligned dielectric boxes

@@ -61,6 +61,19 @@ int ptk_fdtd_graph_create(const ptk_fdtd_params *p, int mode, int unrolled_steps
 int ptk_fdtd_graph_create_host(const ptk_fdtd_params *p, int unrolled_steps, const char *library,
                                unsigned host_fields, ptk_fdtd_graph **out);
 
+/* The same graph with host tasks that use the GPU as a dependent accelerator (hosttask.h:33-144,
+ * task.h:768 BindDependentAcceleratorClass, port.h:1185 BindDependentAccelerator): each host task is
+ * bound to the CUDA class, and its three field inputs and its output to the dependent device, so
+ * the entry point receives device pointers for them and a host pointer for FDTD_PARAMS.
+ * with_streams = 0: entry points have the LPFNDEPHOSTTASK form
+ *   void f(unsigned n, void **args, int *is_dependent, void **device_bindings, unsigned ndeps, void **deps)
+ * and the runtime waits for the device before and after each call;
+ * with_streams = 1: entry points have the LPFNDEPHOSTTASKEX form void f(DEPENDENTCONTEXT *) and order
+ * their work on pStreams[0] (a cudaStream_t), with no host wait.  PTK_ERR_NOTFOUND: library or entry
+ * missing. */
+int ptk_fdtd_graph_create_dephost(const ptk_fdtd_params *p, int unrolled_steps, const char *library,
+                                  unsigned host_fields, int with_streams, ptk_fdtd_graph **out);
+
 /* Push the sticky inputs: per-cell coefficients (Nx*Ny*Nz floats each; all NULL = scalar vacuum
  * coefficients Dt/eps0, Dt/mu0 as in the reference) and the soft Ez source (si<0 or wave NULL = none). */
 int ptk_fdtd_graph_set_problem(ptk_fdtd_graph *g, const float *Ca, const float *Cb, const float *Da,

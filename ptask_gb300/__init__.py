@@ -7,8 +7,8 @@ built: there is no CPU fallback.
 """
 from ._lib import LIB_PATH, PtkError, lib
 from .fdtd import (FIELDS, Problem, Solver, device_info, field_extents, field_shape,
-                   launch_count, random_fields, reference_params, solve, tuned_tiles, zero_fields)
+                   launch_count, random_fields, reference_params, solve, tuned_tiles, default_tiles, zero_fields)
 
 __all__ = ["LIB_PATH", "PtkError", "lib", "FIELDS", "Problem", "Solver", "device_info",
            "field_extents", "field_shape", "launch_count", "random_fields", "reference_params",
-           "solve", "tuned_tiles", "zero_fields"]
+           "solve", "tuned_tiles", "default_tiles", "zero_fields"]

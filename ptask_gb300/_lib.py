@@ -91,6 +91,8 @@ _SIGS = {
     "ptk_stream_create": (C.c_int, [C.POINTER(_P)]),
     "ptk_stream_destroy": (C.c_int, [_P]),
     "ptk_stream_sync": (C.c_int, [_P]),
+    "ptk_device_sync": (C.c_int, []),
+    "ptk_device_ordinal": (C.c_int, [C.POINTER(C.c_int)]),
     "ptk_event_create": (C.c_int, [C.POINTER(_P)]),
     "ptk_event_destroy": (C.c_int, [_P]),
     "ptk_event_record": (C.c_int, [_P, _P]),
@@ -141,6 +143,7 @@ _SIGS = {
     "ptk_server_stats_get": (C.c_int, [_P, C.POINTER(ServerStats)]),
     "ptk_server_destroy": (C.c_int, [_P]),
     "ptk_autotune_tiles":(C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(TileConfig), C.POINTER(C.c_float)]),
+    "ptk_default_tiles": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(TileConfig)]),
     "ptk_selftest_wait_expiry": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_float)]),
     "ptk_problem_generate": (C.c_int, [C.POINTER(ProblemDesc), C.POINTER(FdtdParams), _P, _P, _P, _P,
                                        C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), _P]),

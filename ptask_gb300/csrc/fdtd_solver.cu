@@ -772,4 +772,26 @@ try {
     return PTK_OK;
 } PTK_CATCH_ALL
 
+int ptk_default_tiles(int Nx, int Ny, int Nz, ptk_tile_config *cfg)
+try {
+    clear_error();
+    PTK_CHECK_ARG(cfg, "NULL argument");
+    PTK_CHECK_ARG(Nx >= 1 && Ny >= 1 && Nz >= 1, "grid %dx%dx%d must be at least 1x1x1", Nx, Ny, Nz);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find({Nx, Ny, Nz});
+        if (it != g_tune_cache.end()) {
+            *cfg = it->second.first;
+            return PTK_OK;
+        }
+    }
+    int rc = ensure_init();
+    if (rc) return rc;
+    const int by = 11, stages = 4, vec = yee_bulk_tile_vec(by);
+    int kc = 0;
+    balanced_depths(Nx, Ny, Nz, by, vec, yee_bulk_resident_ctas(by, stages, true), &kc, 1);
+    *cfg = {by, kc, vec, stages};
+    return PTK_OK;
+} PTK_CATCH_ALL
+
 }  // extern "C"

@@ -306,6 +306,23 @@ int ptk_stream_sync(void *stream)
     return PTK_OK;
 }
 
+int ptk_device_sync(void)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    PTK_CUDA_TRY(cudaDeviceSynchronize());
+    return PTK_OK;
+}
+
+int ptk_device_ordinal(int *device)
+{
+    if (!device) return set_error(PTK_ERR_INVALID, "NULL argument");
+    int rc = ensure_init();
+    if (rc) return rc;
+    *device = g_device;
+    return PTK_OK;
+}
+
 int ptk_event_create(void **event)
 {
     int rc = ensure_init();

@@ -241,3 +241,11 @@ def tuned_tiles(nx: int, ny: int, nz: int) -> tuple[int, int, int, int]:
     ms = C.c_float()
     call("ptk_autotune_tiles", nx, ny, nz, C.byref(t), C.byref(ms))
     return t.by, t.kc, t.vec, t.stages
+
+
+def default_tiles(nx: int, ny: int, nz: int) -> tuple[int, int, int, int]:
+    """Tile shape without timing: the autotuner's choice if this process tuned the grid, else the
+    staged material-index kernel's default (11 rows, 4-plane ring, wave-filling depth)."""
+    t = TileConfig()
+    call("ptk_default_tiles", nx, ny, nz, C.byref(t))
+    return t.by, t.kc, t.vec, t.stages

@@ -37,6 +37,7 @@ _SIGS = {
     "ptk_fdtd_graph_destroy": [_P],
     "ptk_fdtd_graph_save": [_P, C.c_char_p],
     "ptk_fdtd_graph_create_host": [C.POINTER(FdtdParams), C.c_int, C.c_char_p, C.c_uint, C.POINTER(_P)],
+    "ptk_fdtd_graph_create_dephost": [C.POINTER(FdtdParams), C.c_int, C.c_char_p, C.c_uint, C.c_int, C.POINTER(_P)],
     "ptk_fdtd_graph_load": [C.POINTER(FdtdParams), C.c_int, C.c_char_p, C.POINTER(_P)],
     "ptk_fdtd_graph_export": [C.POINTER(FdtdParams), C.c_int, C.c_int, C.c_char_p],
     "ptk_graph_xml_roundtrip": [C.c_char_p, C.c_char_p],
@@ -82,6 +83,19 @@ class FDTDGraph:
         h = C.c_void_p()
         _check(rt().ptk_fdtd_graph_create_host(C.byref(params), steps, str(library).encode(), host_fields,
                                                C.byref(h)), "ptk_fdtd_graph_create_host")
+        return cls(params, "unrolled", _handle=h)
+
+    @classmethod
+    def with_dependent_host_tasks(cls, params: FdtdParams, steps: int, library, host_fields: int = 0x3F,
+                                  with_streams: bool = True) -> "FDTDGraph":
+        """The unrolled graph whose tasks for the fields in `host_fields` are host tasks that use the
+        GPU as a dependent accelerator: their field arguments are device pointers.  `with_streams`
+        selects the entry-point form: a DEPENDENTCONTEXT with the stream to order work on
+        (LPFNDEPHOSTTASKEX), or the argument-list form without streams (LPFNDEPHOSTTASK)."""
+        h = C.c_void_p()
+        _check(rt().ptk_fdtd_graph_create_dephost(C.byref(params), steps, str(library).encode(), host_fields,
+                                                  int(bool(with_streams)), C.byref(h)),
+               "ptk_fdtd_graph_create_dephost")
         return cls(params, "unrolled", _handle=h)
 
     @classmethod

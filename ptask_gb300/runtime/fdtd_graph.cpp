@@ -54,6 +54,7 @@ struct ptk_fdtd_graph {
     UINT uid = 0;
     std::string host_library;   // unrolled graph: tasks of the fields in host_fields are host tasks
     unsigned host_fields = 0;
+    int dep_form = 0;           // host tasks with the GPU as dependent accelerator: 1 LPFNDEPHOSTTASK, 2 ...EX
 };
 
 namespace {
@@ -75,6 +76,12 @@ Task *field_task(ptk_fdtd_graph *G, const char *kernel, const char *task, int ou
     // A host task's geometry is the number of times its entry point runs (hosttask.cpp:330-338):
     // once, since the entry point updates the whole field.
     if (host) t->SetComputeGeometry(1, 1, 1);
+    if (host && G->dep_form) {
+        // the field blocks live on the dependent GPU; FDTD_PARAMS stays a host value
+        if (!t->BindDependentAcceleratorClass(ACCELERATOR_CLASS_CUDA, 1, G->dep_form == 2 ? TRUE : FALSE)) return nullptr;
+        for (int q = 0; q < 3; ++q) in[q]->BindDependentAccelerator(ACCELERATOR_CLASS_CUDA, 0);
+        out[0]->BindDependentAccelerator(ACCELERATOR_CLASS_CUDA, 0);
+    }
     else t->SetComputeGeometry((int)e[0], (int)e[1], (int)e[2]);
     return t;
 }
@@ -325,6 +332,28 @@ try {
     ptk_fdtd_graph *G = new_graph(p, PTK_GRAPH_UNROLLED, unrolled_steps);
     G->host_library = library;
     G->host_fields = host_fields;
+    if (!build_unrolled(G, unrolled_steps)) {
+        Graph::DestroyGraph(G->g);
+        delete G;
+        return PTK_ERR_NOTFOUND;
+    }
+    start(G);
+    *out = G;
+    return PTK_OK;
+} PTK_GRAPH_CATCH_ALL
+
+int ptk_fdtd_graph_create_dephost(const ptk_fdtd_params *p, int unrolled_steps, const char *library,
+                                  unsigned host_fields, int with_streams, ptk_fdtd_graph **out)
+try {
+    if (!p || !out || !library || p->Nx < 1 || p->Ny < 1 || p->Nz < 1 || unrolled_steps < 1 || host_fields > 0x3Fu ||
+        with_streams < 0 || with_streams > 1)
+        return PTK_ERR_INVALID;
+    Runtime::SetExitOnRuntimeFailure(FALSE);
+    if (PTFAILED(Runtime::Initialize())) return PTK_ERR_CUDA;
+    ptk_fdtd_graph *G = new_graph(p, PTK_GRAPH_UNROLLED, unrolled_steps);
+    G->host_library = library;
+    G->host_fields = host_fields;
+    G->dep_form = with_streams ? 2 : 1;
     if (!build_unrolled(G, unrolled_steps)) {
         Graph::DestroyGraph(G->g);
         delete G;

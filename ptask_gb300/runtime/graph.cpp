@@ -197,6 +197,22 @@ void Task::SetComputeGeometry(int x, int y, int z)
     m_geom_set = true;
 }
 
+BOOL Task::BindDependentAcceleratorClass(ACCELERATOR_CLASS cls, int nRequiredInstances, BOOL bRequestDependentPSObjects)
+{
+    if (!m_kernel || !m_kernel->IsHost()) {
+        Runtime::HandleError("task %s: dependent accelerators are bound to host tasks only", GetTaskName());
+        return FALSE;
+    }
+    if (cls != ACCELERATOR_CLASS_CUDA || nRequiredInstances != 1) {
+        Runtime::HandleError("task %s: dependent accelerator class %d x %d is not available (one CUDA device)",
+                             GetTaskName(), (int)cls, nRequiredInstances);
+        return FALSE;
+    }
+    m_dep_class = cls;
+    m_dep_ps = bRequestDependentPSObjects;
+    return TRUE;
+}
+
 void Task::SetBlockAndGridSize(PTASKDIM3 grid, PTASKDIM3 block)
 {
     // Recorded for inspection; native kernels choose their own launch shape.
@@ -723,8 +739,12 @@ void Graph::dispatch(Task *t)
         }
 
     // Formal parameters in index order: device views for a native kernel, host views for a host
-    // task (whose writes leave the host copy as the only valid one).
+    // task (whose writes leave the host copy as the only valid one).  A host task with a dependent
+    // CUDA accelerator gets device views on the ports bound to it (port.h:1185) and host views on
+    // the others (hosttask.cpp:380-405).
     const bool host = t->GetCompiledKernel()->IsHost();
+    const bool dep = host && t->HasDependentAcceleratorBindings();
+    auto on_device = [&](Port *p) { return !host || (dep && p->HasDependentAcceleratorBinding()); };
     std::vector<std::pair<int, Formal>> formals;
     for (size_t q = 0; q < t->m_inputs.size(); ++q) {
         Port *p = t->m_inputs[q];
@@ -732,7 +752,7 @@ void Graph::dispatch(Task *t)
         Formal f{p, in[q], nullptr, nullptr};
         if (in[q]) {
             if (is_scalar(in[q])) f.host = in[q]->HostBytes();
-            else if (host) f.host = in[q]->GetDataPointer(p->IsInOutParameter(), TRUE);
+            else if (!on_device(p)) f.host = in[q]->GetDataPointer(p->IsInOutParameter(), TRUE);
             else f.dev = in[q]->DeviceView(m_stream, p->IsInOutParameter(), true);
         }
         formals.push_back({(int)p->GetFormalParameterIndex(), f});
@@ -741,7 +761,7 @@ void Graph::dispatch(Task *t)
         Port *p = t->m_outputs[r];
         if (p->GetFormalParameterIndex() == (UINT)-1) continue;
         Formal f{p, out[r], nullptr, nullptr};
-        if (host) f.host = out[r]->GetDataPointer(TRUE, FALSE);
+        if (!on_device(p)) f.host = out[r]->GetDataPointer(TRUE, FALSE);
         else f.dev = out[r]->DeviceView(m_stream, true, false);
         formals.push_back({(int)p->GetFormalParameterIndex(), f});
     }
@@ -752,19 +772,61 @@ void Graph::dispatch(Task *t)
 
     if (host) {
         // Host task (hosttask.cpp:305-340): the arguments are the formal parameters 0..n-1 as host
-        // pointers; the entry point runs once per point of the task's geometry.
+        // pointers (device pointers where bound to the dependent accelerator); the entry point runs
+        // once per point of the task's geometry.
         std::vector<void *> args;
+        std::vector<BOOL> is_dep;
+        std::vector<void *> dev_of;
+        std::vector<Datablock *> blocks;
+        int ordinal = 0;
+        if (dep) ptk_device_ordinal(&ordinal);
+        void *device = reinterpret_cast<void *>((intptr_t)ordinal);
         for (size_t i = 0; i < formals.size(); ++i) {
             if (formals[i].first != (int)i) {
                 Runtime::HandleError("dispatch of host task %s: no formal parameter %zu", t->GetTaskName(), i);
                 args.clear();
                 break;
             }
-            args.push_back(const_cast<void *>(formals[i].second.host));
+            const Formal &f = formals[i].second;
+            const bool d = f.dev != nullptr;
+            args.push_back(d ? f.dev : const_cast<void *>(f.host));
+            is_dep.push_back(d ? TRUE : FALSE);
+            dev_of.push_back(d ? device : nullptr);
+            blocks.push_back(f.block);
         }
         const UINT reps = repeat * std::max(1, t->m_geom.x) * std::max(1, t->m_geom.y) * std::max(1, t->m_geom.z);
-        if (args.size() == formals.size())
-            for (UINT n = 0; n < reps; ++n) t->GetCompiledKernel()->HostFunction()((UINT)args.size(), args.data());
+        if (args.size() == formals.size()) {
+            void *fn = reinterpret_cast<void *>(t->GetCompiledKernel()->HostFunction());
+            if (!dep) {
+                for (UINT n = 0; n < reps; ++n) t->GetCompiledKernel()->HostFunction()((UINT)args.size(), args.data());
+            } else if (t->DependentBindingsRequirePSObjects()) {
+                // LPFNDEPHOSTTASKEX (hosttask.cpp:520-560): the task orders its work on pStreams[0],
+                // this graph's stream, after the views above; no host wait.
+                void *deps[1] = {device};
+                void *streams[1] = {m_stream};
+                DEPENDENTCONTEXT c{};
+                c.cbDependentContext = sizeof(DEPENDENTCONTEXT);
+                c.nArguments = (UINT)args.size();
+                c.nDependentAccelerators = 1;
+                c.ppArguments = args.data();
+                c.ppDatablocks = blocks.data();
+                c.pbIsDependentBinding = is_dep.data();
+                c.pvDeviceBindings = dev_of.data();
+                c.pDependentDevices = deps;
+                c.pStreams = streams;
+                c.lpszTaskName = const_cast<char *>(t->GetTaskName());
+                for (UINT n = 0; n < reps; ++n) reinterpret_cast<LPFNDEPHOSTTASKEX>(fn)(&c);
+            } else {
+                // LPFNDEPHOSTTASK (hosttask.cpp:405-430): no stream is handed over, so the views
+                // are complete before the call and the task's device work is waited for after it.
+                void *deps[1] = {device};
+                ptk_stream_sync(m_stream);
+                for (UINT n = 0; n < reps; ++n)
+                    reinterpret_cast<LPFNDEPHOSTTASK>(fn)((UINT)args.size(), args.data(), is_dep.data(), dev_of.data(),
+                                                          1, deps);
+                ptk_device_sync();
+            }
+        }
         ++m_stats.host_dispatches;
     } else {
         for (UINT n = 0; n < repeat; ++n) {
@@ -780,12 +842,15 @@ void Graph::dispatch(Task *t)
     ++t->m_dispatches;
     ++m_stats.dispatches;
 
-    // Blocks a kernel wrote get a completion event (a host task's writes are already complete).
-    if (!host) {
+    // Blocks written on the device get a completion event (a host task's host writes are already
+    // complete; a dependent host task's device writes are ordered on this stream, or waited for).
+    if (!host || dep) {
         for (size_t q = 0; q < t->m_inputs.size(); ++q)
-            if (t->m_inputs[q]->IsInOutParameter() && in[q] && !is_scalar(in[q])) in[q]->DeviceWritten(m_stream);
+            if (t->m_inputs[q]->IsInOutParameter() && in[q] && !is_scalar(in[q]) && on_device(t->m_inputs[q]))
+                in[q]->DeviceWritten(m_stream);
         for (size_t r = 0; r < out.size(); ++r)
-            if (t->m_outputs[r]->GetFormalParameterIndex() != (UINT)-1) out[r]->DeviceWritten(m_stream);
+            if (t->m_outputs[r]->GetFormalParameterIndex() != (UINT)-1 && on_device(t->m_outputs[r]))
+                out[r]->DeviceWritten(m_stream);
     }
 
     // Control propagation of the general iterator.
@@ -923,10 +988,11 @@ bool Graph::try_lower_cycle(Task *top)
                 plan->solver_params = *P;
                 plan->coef_key.clear();
                 if (rc == PTK_OK) {
-                    ptk_tile_config best{0, 0, 0, 0};
-                    float ms = 0;
-                    if (ptk_autotune_tiles(P->Nx, P->Ny, P->Nz, &best, &ms) == PTK_OK)
-                        ptk_solver_set_tiles(plan->solver, &best);
+                    // the autotuner's shape if this process tuned the grid, else the default
+                    // staged shape: a graph built for one request must not pay for a tuning pass
+                    ptk_tile_config tiles{0, 0, 0, 0};
+                    if (ptk_default_tiles(P->Nx, P->Ny, P->Nz, &tiles) == PTK_OK)
+                        ptk_solver_set_tiles(plan->solver, &tiles);
                 }
             }
         }

@@ -211,6 +211,40 @@ def test_host_task_graph_file_roundtrip(host_library, tmp_path):
     assert_same(got, oracle.step_ref_f32(f, steps, p), "loaded host graph")
 
 
+@pytest.fixture(scope="module", params=[True, False], ids=["with_streams", "without_streams"])
+def dep_host_library(request, tmp_path_factory):
+    """tests/hosttasks/fdtd_dephosttasks.c built against the product's C ABI, in the
+    LPFNDEPHOSTTASKEX (with streams) or LPFNDEPHOSTTASK form."""
+    import subprocess
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    bdir = root / "ptask_gb300" / "_build"
+    out = tmp_path_factory.mktemp("dephosttasks") / "libfdtd_dephosttasks.so"
+    subprocess.run(["gcc", "-O2", "-shared", "-fPIC", "-I", str(root / "include")] +
+                   ([] if request.param else ["-DPTK_LEGACY_FORM"]) +
+                   [str(root / "tests" / "hosttasks" / "fdtd_dephosttasks.c"), "-L", str(bdir), "-lptask_gb300",
+                    "-Wl,-rpath," + str(bdir), "-o", str(out)], check=True)
+    return out, request.param
+
+
+@pytest.mark.parametrize("host_fields", [0x3F, 0x15])
+def test_dependent_host_task_graph_matches_oracle(dep_host_library, host_fields):
+    """Host tasks bound to the GPU as a dependent accelerator (hosttask.h:33-144) get device
+    pointers for the ports bound to it and run the field updates through the C ABI; the graph's
+    result is the oracle's, bit for bit, for every mix with native GPU tasks."""
+    library, with_streams = dep_host_library
+    shape, steps = (20, 14, 6), 3
+    p = P.reference_params(*shape)
+    f = P.random_fields(*shape, seed=67)
+    with FDTDGraph.with_dependent_host_tasks(p, steps, library, host_fields, with_streams) as g:
+        got = g.solve(f, steps)
+        st = g.stats()
+    n_host = bin(host_fields).count("1")
+    assert st["host_dispatches"] == n_host * steps and st["dispatches"] == 6 * steps
+    assert st["kernel_launches"] == (6 - n_host) * steps   # the host tasks' own launches are theirs
+    assert_same(got, oracle.step_ref_f32(f, steps, p), f"dependent host fields {host_fields:#x}")
+
+
 def test_missing_host_library_or_entry(tmp_path, host_library):
     p = P.reference_params(8, 8, 4)
     with pytest.raises(P.PtkError):

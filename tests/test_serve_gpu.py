@@ -88,12 +88,14 @@ def test_continuous_admission_within_budget_and_plain_mode_agrees():
                 np.testing.assert_array_equal(got[q], batched[t][q])
 
 
-def test_plain_graph_dispatch_matches_server():
-    """The per-graph plain arm (one task-wise PTask graph per request) gives the server's results."""
+@pytest.mark.parametrize("mode", ["taskwise", "fused"])
+def test_plain_graph_dispatch_matches_server(mode):
+    """The per-graph plain arms (one PTask graph per request, task-wise or lowered to the fused loop)
+    give the server's results."""
     reqs = poisson_trace(6, rate=2000.0, seed=13, edge=(12, 40), steps=(10, 40))
     reqs.append(Request(reqs[0].nx, reqs[0].ny, reqs[0].nz, 17, 2, 77, arrival=reqs[-1].arrival))  # graph reuse
     got: dict = {}
-    st = graph_dispatch(reqs, time_scale=1.0, mode="taskwise", cache=2, results=got)
+    st = graph_dispatch(reqs, time_scale=1.0, mode=mode, cache=2, results=got)
     assert st["solves"] == len(reqs) and st["p99_latency_s"] >= st["p50_latency_s"] >= 0
     with Server(keep_results=True, chunk_steps=8) as s:
         tickets = [s.submit(r) for r in reqs]
