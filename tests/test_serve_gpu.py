@@ -150,7 +150,7 @@ def test_full_batched_set_matches_oracle(rows):
     benchmark serves), run in one continuous-batching mix with the benchmark's 7-row, 64-wide tiles
     and with the server's default 11-row, 128-wide ones.  A seeded subset of 8 instances, always
     including the largest, is compared with the FP32 oracle (graphfdtd.cpp:314-340 restated) bit for
-    bit; every instance's checksums are compared with its fields."""
+    bit, and the checksums of those instances with their fields."""
     reqs = batched_instances(64, seed=4)
     largest = max(range(len(reqs)), key=lambda q: reqs[q].cell_updates)
     rng = np.random.default_rng(17 + rows)
