@@ -175,3 +175,29 @@ def test_full_batched_set_matches_oracle(rows):
                                                                f"field {P.FIELDS[f]}")
             f64 = got.astype(np.float64)
             assert abs(sums[q][f] - f64.sum()) <= 1e-12 * max(np.abs(f64).sum(), 1e-300)
+
+
+def test_served_trace_matches_oracle():
+    """The first 200 requests of the served workload's Poisson trace (200 req/s, cube edges 24-256,
+    50-1000 steps, the trace the benchmark serves) admitted as they arrive, by HBM budget, with the
+    server's default tiles.  Eight requests, always including the largest (255^3, 971 steps), are
+    compared with the FP32 oracle bit for bit."""
+    reqs = poisson_trace(200, rate=200.0, seed=5)
+    largest = max(range(len(reqs)), key=lambda q: reqs[q].cell_updates)
+    rng = np.random.default_rng(23)
+    pick = sorted({largest, *(int(q) for q in rng.choice(len(reqs), 7, replace=False))})
+    with Server(keep_results=True) as s:
+        tickets = [s.submit(r) for r in reqs]
+        s.run(time_scale=1.0)
+        assert s.stats()["completed"] == len(reqs)
+        fetched = {q: s.fetch(tickets[q]) for q in pick}
+    for q in pick:
+        r = reqs[q]
+        pr = P.Problem.generate(r.nx, r.ny, r.nz, n_boxes=r.n_boxes, eps=r.eps, box=r.box, steps=r.steps,
+                                source_mode=r.source_mode, seed=r.seed)
+        ref = oracle.step_ext_f32(P.zero_fields(r.nx, r.ny, r.nz), r.steps, pr.params, pr.Ca, pr.Cb, pr.Da, pr.Db,
+                                  pr.src, pr.wave)
+        for f in range(6):
+            assert oracle.normwise_error(fetched[q][f], ref[f]) <= 1e-5
+            np.testing.assert_array_equal(fetched[q][f], ref[f], err_msg=f"request {q} ({r.nx}^3 x {r.steps}) "
+                                                                         f"field {P.FIELDS[f]}")
