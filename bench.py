@@ -18,6 +18,8 @@ Courant 0.5, Gaussian Ez source, 1000 steps).  Prints one JSON line (rank 0):
          workload's 200 req/s and one below saturation, each served by continuous batching and by
          every plain one-at-a-time arm (fused server slot, fused graph dispatch, task-wise graph
          dispatch) on the same requests: solves/s, Mcell/s, p50/p99 and the fraction of peak
+  large  the large single-GPU grid (512x512x384, 500 steps) solved from resident fields with the
+         autotuned tiles: Mcell-updates/s and the fraction of peak
 
 --impl reference times the reference's CPU implementation of the path instead (the oracle port; the
 reference's own build needs its source tree, which is absent where this runs) on the same workload,
@@ -445,6 +447,9 @@ def run_ours(args, wl, world, rank, local):
     if world == 1 and not args.no_served and args.workload == "plain256":
         # The workload's other half: batched and served solves/s and p50/p99 against every plain arm.
         line["served"] = served_subrecords(args, rank, local)
+    if world == 1 and not args.no_large and args.workload == "plain256":
+        # The large single-GPU grid, resident, with autotuned tiles.
+        line["large"] = large_subrecord(local)
     if rank == 0:
         print(json.dumps(line), flush=True)
     dist.close()
@@ -541,6 +546,56 @@ def default_rows(kind: str) -> int:
     return 7 if kind == "batched" else 0
 
 
+def large_subrecord(local: int, solves: int = 3) -> dict:
+    """The large workload (512x512x384, 32 boxes, 500 steps) solved from resident zero fields with the
+    autotuned tiles: Mcell-updates/s over `solves` complete solves (CUDA events) and the step kernel
+    against the measured HBM bandwidth at 49 (material index) or 64 bytes per cell update."""
+    import ptask_gb300 as P
+    from ptask_gb300.device import DeviceBuffer, Event
+    wl = WORKLOADS["large"]
+    shape, T = wl["shape"], wl["steps"]
+    prob = P.Problem.generate(*shape, n_boxes=wl["boxes"], eps=wl["eps"], box=wl["box"], steps=T, source_mode=1,
+                              seed=2)
+    tiles = P.tuned_tiles(*shape)
+    zero = P.zero_fields(*shape)
+    dev = [DeviceBuffer.from_array(a) for a in zero]
+    cells = shape[0] * shape[1] * shape[2]
+    with P.Solver(prob.params) as s:
+        s.set_tiles(*tiles)
+        s.set_problem(prob)
+
+        def solve():
+            s.set_fields_device([b.value for b in dev])
+            s.reset_clock()
+            s.run(T)
+
+        solve()   # warm-up
+        clocks = ClockSampler(local)
+        clocks.start()
+        e0, e1 = Event(), Event()
+        e0.record()
+        for _ in range(solves):
+            solve()
+        e1.record()
+        e1.sync()
+        clk = clocks.stop()
+        ms = e0.elapsed_ms(e1) / solves
+        stages, mat = s.kernel()
+    for b in dev:
+        b.free()
+    peak, peak_src = hbm_peak()
+    bpc = BYTES_PER_CELL_MAT if mat else BYTES_PER_CELL
+    achieved = bpc * cells * T / (ms / 1e3) / 1e9
+    return {"workload": wl["desc"], "grid": list(shape), "time_steps": T, "solves": solves,
+            "mcell_updates_per_s": cells * T / (ms / 1e3) / 1e6, "ms_per_solve": ms,
+            "tiles": {"rows": tiles[0], "z_depth": tiles[1], "cells_per_thread": tiles[2], "staged_planes": stages,
+                      "material_index": mat},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_source": peak_src, "algorithmic_bytes_per_cell": bpc,
+                         "basis": "whole solves (step launches, faces, advances) over CUDA-event time"},
+            "clocks": clk}
+
+
 def served_subrecords(args, rank: int, local: int) -> dict:
     """Compact batched and served records for the default bench line (one run of every arm)."""
     from ptask_gb300.serve import batched_instances, poisson_trace
@@ -624,6 +679,8 @@ def main() -> int:
                     help="batched/served: skip the two per-graph plain dispatch arms (fused and task-wise)")
     ap.add_argument("--no-served", action="store_true",
                     help="default line: leave out the batched and served sub-records")
+    ap.add_argument("--no-large", action="store_true",
+                    help="default line: leave out the large-grid (512x512x384) sub-record")
     ap.add_argument("--served-requests", type=int, default=300,
                     help="default line: requests in each served sub-record's trace")
     ap.add_argument("--subsat-rate", type=float, default=60.0,
