@@ -379,11 +379,12 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
             const float ey1v[4] = {ey1.x, ey1.y, ey1.z, ey1.w};
             const float exjv[4] = {exj1.x, exj1.y, exj1.z, exj1.w}, ezjv[4] = {ezj1.x, ezj1.y, ezj1.z, ezj1.w};
             const float dav[4] = {da.x, da.y, da.z, da.w}, dbv[4] = {db.x, db.y, db.z, db.w};
-            // A warp whose rows all lie outside the instance (past Ny in the last tile of a column, or
-            // the halo row of a warm plane) has no H to compute: it skips the arithmetic instead of
-            // running it on zeros, leaving the SM's issue slots to the warps with cells.
+            // In 128-wide tiles a warp is one row: a warp whose row lies outside the instance (past Ny
+            // in the last tile of a column, or the halo row of a warm plane) has no H to compute and
+            // skips the arithmetic instead of running it on zeros, leaving the SM's issue slots to the
+            // warps with cells.  (64-wide tiles keep the unconditional form, measured faster there.)
             float hxn[4] = {0.f, 0.f, 0.f, 0.f}, hyn[4] = {0.f, 0.f, 0.f, 0.f}, hzn[4] = {0.f, 0.f, 0.f, 0.f};
-            if (__any_sync(0xffffffffu, act)) {
+            if (LW != 32 || __any_sync(0xffffffffu, act)) {
 #pragma unroll
                 for (int e = 0; e < 4; ++e) {
                     hxn[e] = yee_b(dav[e], hxv[e], dbv[e], ey1v[e], eyv[e], cz, ezjv[e], ezv[e], cy);
