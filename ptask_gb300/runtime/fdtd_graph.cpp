@@ -441,8 +441,15 @@ try {
         }
     }
     for (int q = 0; q < 4; ++q) {
-        int rc = push_copy(G->coef_in[q], G->coef_t, c[q], n * sizeof(float));
-        if (rc) return rc;
+        // The coefficients are read on the device only (the H and E step kernels of the cyclic
+        // graph): like the fields, they go straight from the caller's array to the block's device
+        // view, with no copy into a host view first.
+        Datablock *b = Runtime::AllocateDatablock(G->coef_t, nullptr, 0, G->coef_in[q]);
+        if (!b) return PTK_ERR_NOMEM;
+        b->UploadFrom(c[q]);
+        const BOOL ok = G->coef_in[q]->Push(b);
+        b->Release();
+        if (!ok) return PTK_ERR_TIMEOUT;
     }
     SourceDesc sd{-1, -1, -1, 0};
     if (wave && nwave > 0 && si >= 0) {
