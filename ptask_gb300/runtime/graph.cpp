@@ -779,7 +779,8 @@ void Graph::dispatch(Task *t)
         std::vector<void *> dev_of;
         std::vector<Datablock *> blocks;
         int ordinal = 0;
-        if (dep) ptk_device_ordinal(&ordinal);
+        if (dep && ptk_device_ordinal(&ordinal) != PTK_OK)
+            Runtime::HandleError("dispatch of host task %s: no dependent device: %s", t->GetTaskName(), ptk_last_error());
         void *device = reinterpret_cast<void *>((intptr_t)ordinal);
         for (size_t i = 0; i < formals.size(); ++i) {
             if (formals[i].first != (int)i) {
@@ -820,11 +821,14 @@ void Graph::dispatch(Task *t)
                 // LPFNDEPHOSTTASK (hosttask.cpp:405-430): no stream is handed over, so the views
                 // are complete before the call and the task's device work is waited for after it.
                 void *deps[1] = {device};
-                ptk_stream_sync(m_stream);
+                if (ptk_stream_sync(m_stream) != PTK_OK)
+                    Runtime::HandleError("dispatch of host task %s: inputs not ready: %s", t->GetTaskName(),
+                                         ptk_last_error());
                 for (UINT n = 0; n < reps; ++n)
                     reinterpret_cast<LPFNDEPHOSTTASK>(fn)((UINT)args.size(), args.data(), is_dep.data(), dev_of.data(),
                                                           1, deps);
-                ptk_device_sync();
+                if (ptk_device_sync() != PTK_OK)
+                    Runtime::HandleError("host task %s: its device work failed: %s", t->GetTaskName(), ptk_last_error());
             }
         }
         ++m_stats.host_dispatches;
