@@ -287,13 +287,14 @@ int instance_depth(const ptk_server *s, int nz)
     return depth_for_cap(nz, s->depth_cap);
 }
 
-// Deepest cap (planes per staged tile) that still gives the work list a few tiles per resident CTA:
+// Deepest cap (planes per staged tile) that still gives the work list eight tiles per resident CTA:
 // deep tiles pay the pipeline fill and the warm plane rarely, but one small instance alone needs
-// shallow tiles to occupy the GPU.
+// shallow tiles to occupy the GPU, and a mix of instances balances its last wave better with more,
+// shorter tiles (on the 64-instance mix eight per CTA beat four, sixteen and thirty-two).
 int choose_depth_cap(const ptk_server *s)
 {
     static const int caps[] = {192, 128, 96, 64, 48, 32, 24, 16, 12, 8};
-    const long long want = 4LL * s->resident;
+    const long long want = 8LL * s->resident;
     for (int cap : caps) {
         long long tiles = 0;
         for (const Inst *in : s->active) {
