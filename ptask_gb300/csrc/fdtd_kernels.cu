@@ -342,6 +342,23 @@ int balanced_depths(int nx, int ny, int nz, int by, int vec, int resident, int *
     return k;
 }
 
+int leftover_depths(int nx, int ny, int nz, int by, int vec, int resident, int *out, int n)
+{
+    if (resident <= 0 || n <= 0 || by <= 0 || vec <= 0) return 0;
+    const long long cols = (long long)((nx + 32 * vec - 1) / (32 * vec)) * ((ny + by - 1) / by);
+    const long long layers = resident / cols, extra = resident - layers * cols;
+    if (layers < 1 || extra < 1) return 0;
+    const long long rounds = (cols + extra - 1) / extra;   // leftover tiles per extra CTA
+    int k = 0;
+    for (int kc = 4; kc < nz && k < n; ++kc) {
+        const long long rest = nz - layers * kc;
+        if (rest <= 0) break;
+        if (rest >= kc) continue;   // a full further layer, not a leftover
+        if (rounds * (rest + 2) <= kc + 1) out[k++] = kc;
+    }
+    return k;
+}
+
 template <int BY, int V>
 static void launch_by_v(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles, int s_offset,
                         int g, cudaStream_t s)

@@ -218,7 +218,7 @@ static int solver_graph(ptk_solver *s, int len, cudaGraphExec_t *out)
     for (int q = 0; q < len && rc == PTK_OK; ++q)
         rc = rs.stages > 0
                  ? launch_yee_step_bulk(s->d_desc, s->d_tile0, 1, s->total_tiles, q, rs.by, rs.stages, grid, s->d_err,
-                                        s->cap, s->d_work, rs.mat)
+                                        s->cap, s->d_work, rs.mat, /*lazy=*/true)
                  : launch_yee_step_v(s->d_desc, s->d_tile0, 1, s->total_tiles, q, s->by, s->vec, 0, s->cap);
     if (rc == PTK_OK && rs.stages > 0) rc = launch_yee_faces_steps(s->d_desc, s->d_face0, 1, s->faces, 0, len, s->cap);
     if (rc == PTK_OK) rc = launch_advance(s->d_desc, 1, len, s->cap);
@@ -698,8 +698,9 @@ try {
         std::vector<int> ks;
         for (int kc : depths)
             if (!(stages > 0 && kc == 8)) ks.push_back(kc);
-        int bal[2];
-        const int nb = balanced_depths(Nx, Ny, Nz, by, vec, resident, bal, 2);
+        int bal[4];
+        int nb = balanced_depths(Nx, Ny, Nz, by, vec, resident, bal, 2);
+        if (stages > 0) nb += leftover_depths(Nx, Ny, Nz, by, vec, resident, bal + nb, 2);
         for (int q = 0; q < nb; ++q)
             if (std::find(ks.begin(), ks.end(), bal[q]) == ks.end()) ks.push_back(bal[q]);
         for (int kc : ks)

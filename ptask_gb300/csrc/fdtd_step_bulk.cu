@@ -102,11 +102,12 @@ template <int BY>
 __host__ __device__ constexpr int warps_of() { return (BY + 1) / rows_per_warp<width_of(BY)>(); }
 template <int BY>
 __host__ __device__ constexpr size_t xchg_bytes() { return (size_t)2 * 2 * (BY + 1) * lanes_per_row<width_of(BY)>() * sizeof(float4); }
-// [S stages][H exchange][material table (MAT)][S mbarriers][tile slot]
-template <int BY, int S, bool MAT>
+// [S stages][H exchange][material table (MAT)][S mbarriers][tile slot][next tile (LAZY)]
+constexpr size_t kTileBytes = 64;
+template <int BY, int S, bool MAT, bool LAZY = false>
 __host__ __device__ constexpr size_t smem_bytes()
 {
-    return S * stage_bytes<BY, MAT>() + xchg_bytes<BY>() + (MAT ? kTabBytes : 0) + S * 8 + 16;
+    return S * stage_bytes<BY, MAT>() + xchg_bytes<BY>() + (MAT ? kTabBytes : 0) + S * 8 + 16 + (LAZY ? kTileBytes : 0);
 }
 
 // Map of array a for field parity par in an instance's map set.
@@ -186,7 +187,15 @@ __device__ __forceinline__ bool tile_at(int t, const InstDesc *__restrict__ inst
 // by k_yee_faces_steps.  A CTA streams its tiles' planes through one continuous ring: it knows its
 // next tile while it works on the current one, and once the current tile's planes are all in
 // flight the refills continue with the next tile's, so a tile starts without a pipeline fill.
-template <int BY, int S, bool MAT>
+//
+// When the next tile is claimed from the work counter: EAGER (LAZY false) as soon as the current
+// one starts, which keeps the claim's latency (an atomic, a search over the instances) off the
+// plane loop of the many shallow tiles of a served mix; LAZY just before the ring reaches the next
+// tile's first plane, so that CTAs that run ahead take the remaining tiles.  The single-instance
+// solver uses LAZY: its grids can then be cut into layers that occupy all but a few resident CTAs
+// plus a thin last layer that those few work through meanwhile (an eager CTA would claim a
+// last-layer tile at the start and run it after its own layer tile).
+template <int BY, int S, bool MAT, bool LAZY = false>
 __global__ void __launch_bounds__(32 * warps_of<BY>(), ctas_per_sm(BY))
 k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile0, int ninst, int s_off,
                 int total_tiles, int *err, int *work)
@@ -201,6 +210,9 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
     float4 *tab = reinterpret_cast<float4 *>(smem + S * SB + xchg_bytes<BY>());   // MAT: (Ca, Cb, Da, Db)[256]
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + S * SB + xchg_bytes<BY>() + (MAT ? kTabBytes : 0));
     int *slot = reinterpret_cast<int *>(bars + S);   // next tile, handed to the whole CTA
+    // LAZY: the claimed tile's descriptor; only warp 0 reads it (to issue its planes) until it
+    // becomes the current tile, so it holds no registers in the plane loop.
+    Tile *sT1 = reinterpret_cast<Tile *>(bars + S + 2);
     const void *tab_src = nullptr;                   // instance whose table is loaded (MAT)
 
     const int lane = threadIdx.x, ty = threadIdx.y;
@@ -234,11 +246,16 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
 
     int t = blockIdx.x, t1 = total_tiles;
     Tile T0{}, T1{};
-    bool have0 = fetch(t, T0), have1 = false;
-    if (have0) {
-        t1 = advance(t);
-        have1 = fetch(t1, T1);
+    bool have0 = fetch(t, T0), have1 = false, asked1 = false;
+    if constexpr (!LAZY) {
+        if (have0) {
+            t1 = advance(t);
+            have1 = fetch(t1, T1);
+        }
     }
+    auto next_tile = [&]() -> const Tile & {
+        if constexpr (LAZY) return *sT1; else return T1;
+    };
     // Ring positions: the planes of this CTA's tiles in order; plane j of the current tile is
     // position gbase + j.  Positions below `issued` are in flight or consumed.
     unsigned gbase = 0, issued = 0;
@@ -256,7 +273,8 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
                 const int j = (int)(p - gbase);
                 issue_plane<BY, MAT>(T0.maps, T0.par, T0.x0, T0.y0, T0.kstart + j, T0.kstart + j == T0.k1,
                                      stages + (size_t)(p % S) * SB, &bars[p % S], lane);
-            } else if (have1 && p < gbase + (unsigned)(T0.nplanes + T1.nplanes)) {
+            } else if (have1 && p < gbase + (unsigned)(T0.nplanes + next_tile().nplanes)) {
+                const Tile &T1 = next_tile();
                 if (!acq1) {
                     if (lane < n_arrays<MAT>()) tma_acquire(map_of<MAT>(T1.maps, lane, T1.par));
                     acq1 = true;
@@ -416,6 +434,17 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
                 sH[(BY + 1) * LW + r * LW + lx] = make_float4(hzn[0], hzn[1], hzn[2], hzn[3]);
             }
             __syncthreads();
+            if constexpr (LAZY) {
+                // the refill below reaches the next tile's first plane from q = nplanes - S on
+                if (!asked1 && q == max(0, T0.nplanes - S)) {
+                    t1 = advance(t);
+                    Tile Tn;
+                    have1 = fetch(t1, Tn);
+                    if (ty == 0 && lane == 0 && have1) *sT1 = Tn;
+                    __syncwarp();   // warp 0 reads it in the refill below
+                    asked1 = true;
+                }
+            }
             // Plane k's stage was read (as "next") before the previous barrier and (as "current")
             // before this one, and nothing after this barrier reads a stage: refill it now (with a
             // plane of the next tile once this tile's planes are all in flight).
@@ -471,15 +500,32 @@ k_yee_step_bulk(const InstDesc *__restrict__ insts, const int *__restrict__ tile
         // The stages of this tile are refilled only after the barriers of the planes that follow
         // them, which every thread reaches after finishing this tile.
         __syncthreads();
-        T0 = T1;
-        have0 = have1;
-        acq0 = acq1;
-        acq1 = false;
-        have1 = false;
-        if (have0) {
-            t = t1;
-            t1 = advance(t);
-            have1 = fetch(t1, T1);
+        if constexpr (LAZY) {
+            if (!asked1) {   // not reached: the plane loop claims it (q = nplanes - S <= nplanes - 2)
+                t1 = advance(t);
+                Tile Tn;
+                have1 = fetch(t1, Tn);
+                if (ty == 0 && lane == 0 && have1) *sT1 = Tn;
+                __syncthreads();
+            }
+            if (have1) T0 = *sT1;   // written before this tile's last barrier
+            have0 = have1;
+            acq0 = acq1;
+            acq1 = false;
+            have1 = false;
+            asked1 = false;
+            if (have0) t = t1;
+        } else {
+            T0 = T1;
+            have0 = have1;
+            acq0 = acq1;
+            acq1 = false;
+            have1 = false;
+            if (have0) {
+                t = t1;
+                t1 = advance(t);
+                have1 = fetch(t1, T1);
+            }
         }
     }
     // Every issued plane has normally been waited for.  If a wait expired, let the copies still
@@ -556,42 +602,42 @@ int launch_yee_faces_steps(const InstDesc *d_insts, const long long *d_face0, in
 long long face_nodes(int nx, int ny, int nz) { return (long long)ny * nz + (long long)nx * nz + (long long)nx * ny; }
 
 // Opt the instantiation into its dynamic shared memory (once per process; repeating it is harmless).
-template <int BY, int S, bool MAT>
+template <int BY, int S, bool MAT, bool LAZY>
 static int prepare_bulk()
 {
     static bool attr_set = false;
     if (!attr_set) {
-        PTK_CUDA_TRY(cudaFuncSetAttribute(k_yee_step_bulk<BY, S, MAT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)smem_bytes<BY, S, MAT>()));
+        PTK_CUDA_TRY(cudaFuncSetAttribute(k_yee_step_bulk<BY, S, MAT, LAZY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem_bytes<BY, S, MAT, LAZY>()));
         // all of the unified L1 / shared storage as shared memory, so small rings can co-reside
-        PTK_CUDA_TRY(cudaFuncSetAttribute(k_yee_step_bulk<BY, S, MAT>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                          100));
+        PTK_CUDA_TRY(cudaFuncSetAttribute(k_yee_step_bulk<BY, S, MAT, LAZY>,
+                                          cudaFuncAttributePreferredSharedMemoryCarveout, 100));
         attr_set = true;
     }
     return PTK_OK;
 }
 
-template <int BY, int S, bool MAT>
+template <int BY, int S, bool MAT, bool LAZY>
 static int resident_bulk()
 {
-    if (prepare_bulk<BY, S, MAT>()) return 0;
+    if (prepare_bulk<BY, S, MAT, LAZY>()) return 0;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_yee_step_bulk<BY, S, MAT>, 32 * warps_of<BY>(),
-                                                      smem_bytes<BY, S, MAT>()) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_yee_step_bulk<BY, S, MAT, LAZY>, 32 * warps_of<BY>(),
+                                                      smem_bytes<BY, S, MAT, LAZY>()) != cudaSuccess)
         return 0;
     return per_sm * std::max(1, sm_count());
 }
 
-template <int BY, int S, bool MAT>
+template <int BY, int S, bool MAT, bool LAZY>
 static int launch_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles, int s_offset,
                        int grid, int *err, int *work, cudaStream_t s)
 {
-    const size_t smem = smem_bytes<BY, S, MAT>();
-    int rc = prepare_bulk<BY, S, MAT>();
+    const size_t smem = smem_bytes<BY, S, MAT, LAZY>();
+    int rc = prepare_bulk<BY, S, MAT, LAZY>();
     if (rc) return rc;
     const int g = (grid <= 0 || grid > total_tiles) ? total_tiles : grid;
-    k_yee_step_bulk<BY, S, MAT><<<g, dim3(32, warps_of<BY>()), smem, s>>>(d_insts, d_tile0, ninst, s_offset, total_tiles,
-                                                                  err, work);
+    k_yee_step_bulk<BY, S, MAT, LAZY><<<g, dim3(32, warps_of<BY>()), smem, s>>>(d_insts, d_tile0, ninst, s_offset,
+                                                                                total_tiles, err, work);
     PTK_CUDA_TRY(cudaGetLastError());
     count_launches(1);
     return PTK_OK;
@@ -599,7 +645,8 @@ static int launch_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, i
 
 // Instantiated shapes (rows, ring stages).  Rings of at least 2 stages: plane q waits for the stage
 // of plane q+1 before its barrier, and the stage of plane q+1 is issued after the barrier of plane
-// q+1-S, so q+1-S <= q-1.  The material-index stages are smaller, so deeper rings fit.
+// q+1-S, so q+1-S <= q-1.  The material-index stages are smaller, so deeper rings fit.  The
+// material-index shapes also come with the late next-tile claim (the solver's form).
 #define PTK_DENSE_SHAPES(X) X(4, 2, false) X(4, 3, false) X(4, 4, false) X(4, 5, false) \
     X(8, 2, false) X(8, 3, false) X(8, 4, false) X(10, 3, false) X(11, 3, false)
 #define PTK_MAT_SHAPES(X) X(4, 2, true) X(4, 3, true) X(4, 4, true) X(4, 5, true) X(4, 6, true) \
@@ -608,12 +655,19 @@ static int launch_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, i
     X(7, 3, true) X(7, 4, true)
 
 int launch_yee_step_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles, int s_offset,
-                         int by, int stages, int grid, int *err, cudaStream_t s, int *work, bool mat)
+                         int by, int stages, int grid, int *err, cudaStream_t s, int *work, bool mat, bool lazy)
 {
     if (total_tiles <= 0) return PTK_OK;
+    if (lazy && mat) {
+#define PTK_BULK_L(B, S, M)                                                                           \
+    if (by == B && stages == S && mat == M)                                                           \
+        return launch_bulk<B, S, M, true>(d_insts, d_tile0, ninst, total_tiles, s_offset, grid, err, work, s);
+        PTK_MAT_SHAPES(PTK_BULK_L)
+#undef PTK_BULK_L
+    }
 #define PTK_BULK(B, S, M)                                                                               \
     if (by == B && stages == S && mat == M)                                                             \
-        return launch_bulk<B, S, M>(d_insts, d_tile0, ninst, total_tiles, s_offset, grid, err, work, s);
+        return launch_bulk<B, S, M, false>(d_insts, d_tile0, ninst, total_tiles, s_offset, grid, err, work, s);
     PTK_DENSE_SHAPES(PTK_BULK) PTK_MAT_SHAPES(PTK_BULK)
 #undef PTK_BULK
     return set_error(PTK_ERR_INVALID, "no staged kernel for %d rows x %d stages%s", by, stages,
@@ -625,7 +679,7 @@ int yee_bulk_tile_vec(int by) { return width_of(by) / 32; }
 size_t yee_bulk_smem_bytes(int by, int stages, bool mat)
 {
 #define PTK_SM(B, S, M) \
-    if (by == B && stages == S && mat == M) return smem_bytes<B, S, M>();
+    if (by == B && stages == S && mat == M) return smem_bytes<B, S, M, false>();
     PTK_DENSE_SHAPES(PTK_SM) PTK_MAT_SHAPES(PTK_SM)
 #undef PTK_SM
     return 0;
@@ -634,7 +688,7 @@ size_t yee_bulk_smem_bytes(int by, int stages, bool mat)
 int yee_bulk_resident_ctas(int by, int stages, bool mat)
 {
 #define PTK_RES(B, S, M) \
-    if (by == B && stages == S && mat == M) return resident_bulk<B, S, M>();
+    if (by == B && stages == S && mat == M) return resident_bulk<B, S, M, false>();
     PTK_DENSE_SHAPES(PTK_RES) PTK_MAT_SHAPES(PTK_RES)
 #undef PTK_RES
     return 0;

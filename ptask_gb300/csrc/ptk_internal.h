@@ -126,9 +126,11 @@ int launch_yee_step_v(const InstDesc *d_insts, const int *d_tile0, int ninst, in
 // raised if a bounded wait expires.  With `work` (one zeroed counter per step offset), CTAs past
 // the first wave take tiles in list order as they free up instead of a static stride.  With `mat`
 // every instance carries a material index (and its map) and the coefficients come from its table.
+// With `lazy` (material-index shapes), each CTA claims its next tile from `work` just before the
+// ring needs it instead of when the current one starts (the single-instance solver's form).
 int launch_yee_step_bulk(const InstDesc *d_insts, const int *d_tile0, int ninst, int total_tiles, int s_offset,
                          int by, int stages, int grid, int *err, cudaStream_t s, int *work = nullptr,
-                         bool mat = false);
+                         bool mat = false, bool lazy = false);
 // The face H nodes (Hx at i = Nx, Hy at j = Ny, Hz at k = Nz) of every instance advanced by `len`
 // steps from step offset s_offset in one launch; the staged kernel's tile lists leave them out
 // (descriptors planned with face_tiles = 0).  d_face0: ninst + 1 prefix sums of face_nodes().
@@ -145,6 +147,10 @@ int yee_bulk_resident_ctas(int by, int stages, bool mat = false);
 // Z depths (at most `n`, best first) whose tile count fills whole waves of `resident` CTAs with the
 // least work per CTA: each CTA's cost is its planes plus the warm plane and the pipeline fill.
 int balanced_depths(int nx, int ny, int nz, int by, int vec, int resident, int *out, int n);
+// Z depths (at most `n`, shallowest first) that fill `resident` CTAs with whole layers of tiles
+// and leave a thin last layer: the CTAs beyond those layers work through the last layer's tiles
+// while the layers run, so every layer tile is shallower than one depth covering the grid.
+int leftover_depths(int nx, int ny, int nz, int by, int vec, int resident, int *out, int n);
 // CTAs of the step kernel with `by` rows (and `vec`) that fit on the whole GPU at once.
 int yee_resident_ctas(int by);
 int yee_resident_ctas(int by, int vec);
