@@ -539,11 +539,12 @@ def served_desc(n, rate):
             "cube edge log-uniform in [24,256], steps uniform in [50,1000], FP32, admission by HBM budget")
 
 
-# Staged tile shape per workload, as measured on GB300 (same box, alternating runs): the batched mix
-# (x extents 32-192) runs 3.6 % faster on 7-row, 64-wide tiles; the served mix (cubes up to 256) 17 %
-# faster on the server's default 11-row, 128-wide tiles.
+# Staged tile shape per workload, as measured on GB300 (same box, two runs each): the batched mix
+# (x extents 32-192) serves 66.6 solves/s on 23-row, 64-wide tiles (twelve warps, one CTA per SM)
+# against 64.1 on 7-row and 60.2 on 11-row tiles; the served mix (cubes up to 256) 76.3 on the
+# server's default 11-row, 128-wide tiles against 69.2 on 23-row and 67.3 on 7-row tiles.
 def default_rows(kind: str) -> int:
-    return 7 if kind == "batched" else 0
+    return 23 if kind == "batched" else 0
 
 
 def large_subrecord(local: int, solves: int = 3) -> dict:
@@ -666,7 +667,7 @@ def main() -> int:
     ap.add_argument("--rate", type=float, default=200.0,
                     help="served workload: Poisson arrival rate, requests/s (200: the workload's rate)")
     ap.add_argument("--server-rows", type=int, default=0,
-                    help="batched / served: staged tile rows (0: 7 for batched, the server's default 11 for "
+                    help="batched / served: staged tile rows (0: 23 for batched, the server's default 11 for "
                          "served; 7 and 23 give 64-wide tiles)")
     ap.add_argument("--tiles", default=None, help="fixed tile shape ROWS,DEPTH (skips the autotuner)")
     ap.add_argument("--no-autotune", action="store_true")

@@ -144,11 +144,11 @@ def test_many_work_lists_evict_cached_graphs_and_stay_exact():
                 np.testing.assert_array_equal(got[f], ref[f], err_msg=f"request {q} field {P.FIELDS[f]}")
 
 
-@pytest.mark.parametrize("rows", [7, 0])
+@pytest.mark.parametrize("rows", [23, 7, 0])
 def test_full_batched_set_matches_oracle(rows):
     """The whole 64-instance batched workload (per-axis edges 32-192, 100-2000 steps, the set the
-    benchmark serves), run in one continuous-batching mix with the benchmark's 7-row, 64-wide tiles
-    and with the server's default 11-row, 128-wide ones.  A seeded subset of 8 instances, always
+    benchmark serves), run in one continuous-batching mix with the benchmark's 23-row, 64-wide tiles,
+    the 7-row, 64-wide ones and the server's default 11-row, 128-wide ones.  A seeded subset of 8 instances, always
     including the largest, is compared with the FP32 oracle (graphfdtd.cpp:314-340 restated) bit for
     bit, and the checksums of those instances with their fields."""
     reqs = batched_instances(64, seed=4)
