@@ -238,6 +238,24 @@ def test_full_size_first_steps_match_oracle(full_problem):
     assert_parity(got, ref, "256^3 x 3")
 
 
+@pytest.mark.parametrize("tiles", [(11, 82, 4, 4), (23, 82, 2, 4), (11, 84, 4, 4)])
+def test_full_size_thin_last_layer_matches_oracle(full_problem, tiles):
+    """256^3 cut into three layers of 82 or 84 planes that occupy 144 of the resident CTAs and a thin
+    last layer of 4-10 planes that the remaining CTAs claim one tile after another while the layers
+    run (the solver's late tile claim); 12 steps, bit for bit against the oracle."""
+    pr = full_problem
+    f = P.random_fields(*FULL, seed=43, scale=1e-3)
+    steps = 12
+    ref = oracle.step_ext_f32(f, steps, pr.params, pr.Ca, pr.Cb, pr.Da, pr.Db, pr.src, pr.wave)
+    with P.Solver(pr.params) as s:
+        s.set_tiles(*tiles)
+        s.set_problem(pr)
+        s.set_fields(f)
+        s.run(steps)
+        assert s.kernel() == (4, True)
+        assert_parity(s.get_fields(), ref, f"256^3 x {steps}, tiles {tiles}")
+
+
 def test_full_size_full_length_matches_oracle(full_problem):
     """The plain-graph workload itself (256^3, 1000 steps from zero fields) with the autotuned
     tiles, bit for bit against the FP32 oracle."""
