@@ -34,9 +34,12 @@ def test_unrolled_reference_graph(shape, steps, tmp_path):
     assert dot.count("ComTask_") >= 6 * steps
 
 
-def test_unrolled_pipelined_instances():
-    """numBlocks instances pushed back to back (graphfdtd.cpp:1076-1097): every result equals one solve."""
-    shape, steps, n = (16, 12, 4), 4, 4
+@pytest.mark.parametrize("n", [4, 24])
+def test_unrolled_pipelined_instances(n):
+    """numBlocks instances pushed back to back (graphfdtd.cpp:1076-1097): every result equals one solve.
+    With 24 instances the pushes outrun the graph's capacity-4 channels and block until it drains
+    them (the pipelining stress of ptaskUnitTest/pipelinestresstest.cpp)."""
+    shape, steps = (16, 12, 4), 4
     p = P.reference_params(*shape)
     f = P.random_fields(*shape, seed=52)
     with FDTDGraph(p, "unrolled", unrolled_steps=steps) as g:
@@ -45,6 +48,37 @@ def test_unrolled_pipelined_instances():
     ref = oracle.step_ref_f32(f, steps, p)
     for r in res:
         assert_same(r, ref, "pipelined")
+
+
+def test_graphs_run_concurrently_from_two_threads():
+    """Two graphs of different shapes, each driven from its own host thread at the same time (the
+    runtime's concurrency stress, as in ptaskUnitTest/rttests.cpp): both results bit-exact."""
+    import threading
+
+    cases = [((40, 28, 20), 23, "fused", 91), ((33, 45, 18), 17, "taskwise", 92)]
+    out, errs = {}, []
+
+    def run(shape, steps, mode, seed):
+        try:
+            pr = P.Problem.generate(*shape, n_boxes=2, eps=(1, 9), box=(4, 12), steps=steps, seed=seed)
+            f = P.random_fields(*shape, seed=seed + 100, scale=1e-3)
+            with FDTDGraph(pr.params, mode) as g:
+                g.set_problem(pr)
+                res = [g.solve(f, steps) for _ in range(3)]
+            out[seed] = (pr, f, steps, res)
+        except Exception as e:   # reported below, on the test's thread
+            errs.append(e)
+
+    threads = [threading.Thread(target=run, args=c) for c in cases]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errs, errs
+    for seed, (pr, f, steps, res) in out.items():
+        ref = oracle.step_ext_f32(f, steps, pr.params, pr.Ca, pr.Cb, pr.Da, pr.Db, pr.src, pr.wave)
+        for got in res:
+            assert_same(got, ref, f"concurrent graph {seed}")
 
 
 @pytest.mark.parametrize("mode", ["fused", "captured", "taskwise"])
