@@ -5,9 +5,10 @@ The reference stresses its runtime's setup and teardown with repeated create-run
 path (the unrolled and cyclic PTask graphs in each lowering, the resident solver, the serving
 engine) is created, used and destroyed several times; after the first cycle, which may set up
 process-wide state once (pinned staging, autotuned shapes, kernel attributes), the device pool's
-used bytes are back where they started after every cycle, and every result matches the oracle.
+used bytes never grow from one cycle to the next, and every result matches the oracle.
 """
 import ctypes as C
+import gc
 
 import numpy as np
 import pytest
@@ -22,6 +23,7 @@ pytestmark = pytest.mark.gpu
 
 
 def pool_used() -> int:
+    gc.collect()   # objects left by earlier tests are freed now, not in the middle of the check
     _lib.call("ptk_device_sync")
     reserved, used = C.c_size_t(), C.c_size_t()
     _lib.call("ptk_pool_stats", C.byref(reserved), C.byref(used))
@@ -69,4 +71,4 @@ def test_create_use_destroy_cycles_leave_no_device_memory():
         assert pool_used() > base
     for _ in range(3):
         one_cycle()
-        assert pool_used() == base, "device memory left allocated after graphs, solvers and servers were destroyed"
+        assert pool_used() <= base, "device memory left allocated after graphs, solvers and servers were destroyed"
